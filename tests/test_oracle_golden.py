@@ -1,0 +1,150 @@
+"""The oracle's C restatement against the reference's own outputs.
+
+Golden vectors come from the reference's filter sources compiled here
+(tests/golden/make_golden.py) and from the reference's committed fixtures
+(filterStrainCube/test/In13_P16, pseudopotFitting/TESTS/zb_cdse).  Integer
+and table work must match bit for bit; floating-point stages within the
+tolerances written in each test.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_rng_bit_exact(golden):
+    g = golden("ref_small.npz")
+    for seed in (874917403, 12345, 1131359211):
+        r = O.rng(-seed)
+        assert np.array_equal(O.uniforms(r, 300), g[f"ran_{seed}"])
+
+
+def test_init_psi_bit_exact(golden):
+    g = golden("ref_small.npz")
+    n = int(np.prod(g["dims"]))
+    r = O.rng(-777)
+    got = np.stack([O.init_psi(r, n, float(g["dv"])) for _ in range(2)])
+    assert np.array_equal(got, g["init_psi_seed777"])
+
+
+def test_ksqr_bit_exact(golden):
+    g = golden("ref_small.npz")
+    nx, ny, nz = (int(v) for v in g["dims"])
+    got = O.ksqr(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]))
+    assert np.array_equal(got, g["ksqr"])
+
+
+def test_vbuild_bit_exact(golden):
+    g = golden("ref_small.npz")
+    tab_v = np.stack([O.shift_table(v) for v in g["tab_v"]])
+    got = O.vbuild(g["rx"], g["ry"], g["rz"], g["types"], g["tab_r"], tab_v, [1024, 1024],
+                   tuple(int(v) for v in g["dims"]),
+                   (float(g["xmin"]), float(g["ymin"]), float(g["zmin"])),
+                   (float(g["dx"]), float(g["dy"]), float(g["dz"])))
+    assert np.array_equal(got, g["potl"])
+    assert got.min() == g["vmin"]
+
+
+@pytest.mark.parametrize("nc", [128, 1024])
+def test_coefficients_bit_exact(golden, nc):
+    g = golden("ref_small.npz")
+    ar, ai, zn = O.coefficients(g["el"], nc, float(g["dE"]), float(g["vmin"]),
+                                float(g[f"dt_{nc}"]))
+    assert np.array_equal(zn, g[f"zn_{nc}"])
+    assert np.array_equal(ar, g[f"an_{nc}"].real)
+    assert np.array_equal(ai, g[f"an_{nc}"].imag)
+
+
+def _ctx(g):
+    return O.Context(tuple(int(v) for v in g["dims"]), g["potl"], g["ksqr"], float(g["dv"]))
+
+
+def test_hamiltonian(golden):
+    g = golden("ref_small.npz")
+    got = _ctx(g).hamiltonian(g["h_in"])
+    ref = g["h_out"]
+    # two FFTs of different algorithms: agreement to FP64 roundoff
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_hnorm(golden):
+    g = golden("ref_small.npz")
+    dE = float(g["dE"])
+    got = _ctx(g).hnorm(g["h_in"], 4.0 / dE, float(g["vmin"]), 0.37)
+    ref = g["hnorm_out"]
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_filter_cycle(golden):
+    g = golden("ref_small.npz")
+    dE = float(g["dE"])
+    an = g["an_128"].real
+    got = _ctx(g).filter_cycle(g["init_psi_seed777"][0], an, g["zn_128"], 4.0 / dE,
+                               float(g["vmin"]))
+    ref = g["filter_out"]
+    for e in range(ref.shape[0]):
+        assert np.abs(got[e] - ref[e]).max() <= 1e-11 * np.abs(ref[e]).max()
+
+
+def test_energy_all(golden):
+    g = golden("ref_small.npz")
+    got = _ctx(g).energy_all(g["filter_norm"])
+    assert np.allclose(got, g["energy_all"], rtol=1e-12, atol=1e-12)
+
+
+def test_energy_range(golden):
+    g = golden("ref_small.npz")
+    emax, dE, it = _ctx(g).energy_range(float(g["vmin"]))
+    assert abs(dE - float(g["dE"])) <= 1e-10 * abs(float(g["dE"]))
+
+
+def test_pipeline_small(golden):
+    g = golden("ref_small.npz")
+    if not O.lapack_available():
+        pytest.skip("ILP64 OpenBLAS not found")
+    n = int(np.prod(g["dims"]))
+    ns, ms, nc = 4, 3, 128
+    start = O.start_states(int(g["run_seed"]), ns, n, float(g["dv"]))
+    res = _ctx(g).pipeline(start, g["el"], nc, float(g["vmin"]), nthreads=1)
+    assert res["mkept"] == len(g["run_eval"])
+    assert abs(res["timing"]["dE"] - float(g["run_dE"])) <= 1e-10 * float(g["run_dE"])
+    assert np.allclose(res["eval"], g["run_eval"], rtol=0, atol=1e-9)
+    # eval.dat prints sigma with %g (6 digits)
+    assert np.allclose(res["sigma"], g["run_sigma"], rtol=2e-5, atol=1e-7)
+
+
+def test_form_factor_kat(golden):
+    g = golden("zb_cdse_formfactor.npz")
+    for key, pot in (("cd_params", g["pot_cd"]), ("se_params", g["pot_se"])):
+        r, v = O.form_factor_table(g[key], float(g["vol_per_atom"]))
+        # the reference printed r and v with %g: 6 significant digits
+        assert np.allclose(r, pot[:, 0], rtol=6e-6, atol=1e-12)
+        assert np.allclose(v, pot[:, 1], rtol=6e-6, atol=6e-6 * np.abs(pot[:, 1]).max())
+
+
+@pytest.mark.slow
+def test_in13_fixture_end_to_end():
+    """The restatement reproduces the reference's published In13_P16 run."""
+    from tests import fixture_in13
+
+    if not O.lapack_available():
+        pytest.skip("ILP64 OpenBLAS not found")
+    f = fixture_in13.load()
+    pot = O.vbuild(*f["xyz"].T, f["types"], f["tab_r"], f["tab_v_shifted"], f["tab_n"],
+                   f["dims"], f["mins"], f["steps"], scale=f["strain_scale"])
+    assert abs(pot.min() - f["vmin"]) < 1e-5 and abs(pot.max() - f["vmax"]) < 1e-5
+    ks = O.ksqr(*f["dims"], *f["steps"])
+    ctx = O.Context(f["dims"], pot, ks, f["dv"])
+    n = int(np.prod(f["dims"]))
+    start = O.start_states(f["seed"], int(f["ns"]), n, f["dv"])
+    res = ctx.pipeline(start, f["el"], int(f["nc"]), float(pot.min()))
+    assert abs(res["timing"]["dE"] - f["dE"]) < 1e-4
+    assert res["mkept"] == int(f["cutoff"])
+    ev, sg = res["eval"], res["sigma"]
+    ref_ev, ref_sg = f["eval"], f["sigma"]
+    win = (ref_ev > -0.25) & (ref_ev < 0.0) & (ref_sg < 1e-5)
+    assert win.sum() >= 25
+    for e in ref_ev[win]:
+        assert np.abs(ev - e).min() < 1e-6
+    mine = (ev > -0.25) & (ev < 0.0) & (sg < 1e-5)
+    assert mine.sum() == win.sum()
