@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""Benchmark of the filter-diagonalisation path on one GB300 (or N replicas).
+
+Workload (BASELINE config 1): zincblende CdSe-like sphere of radius 2.5 nm
+(2317 atoms, seeded form factors), 128^3 grid, 64 start states x 8 target
+energies, Newton filter length 1024, the filter's H psi chain in complex64
+with FP32 accumulation.  Synthetic inputs (no dataset is involved).
+
+One step = the whole Newton filter (filter/filter.c:59-83) of the 64 start
+states: 64 x 1023 Hamiltonian applies.  Metric: H psi applies per second.
+  value : inputs resident in HBM, device pointers (sep_filter_dev), CUDA
+          events on the library's stream.
+  e2e   : the public host-pointer call (sep_filter) from pinned host memory:
+          start states in, filtered states out, every step.
+Extra keys: the plain FP64 filter rate (same workload, bounded sample), the
+time to band-edge eigenpairs of the whole path (sep_pipeline), the roofline of
+the dominant kernel, the oracle's CPU filter on the host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl sep|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="r2.5nm_128", radius_nm=2.5, n=128, ms=8, ns=64, nc=1024, seed=11,
+                elmin=-0.4, elmax=-0.1)
+START_SEED = -271828
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="sep", choices=["sep", "reference"])
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip FP64 sample, pipeline, roofline and CPU baseline")
+    p.add_argument("--profile", choices=["mixed", "f64"], default=None,
+                   help="run only a small filter case for an ncu capture: 24 start states "
+                        "x 8 Newton steps of the 128^3 workload (about 3.5 GB on the device)")
+    return p.parse_args()
+
+
+def run_profile(args):
+    """Small case of the same kernels for ncu (one GPU, a few GB)."""
+    import semi_empirical_pseudopotentials_gb300 as sep
+
+    S = build_system()
+    tr, tv = tables(sep, S)
+    ctx = sep.Context(S.dims, S.steps, precision=args.profile)
+    ctx.set_block_steps(8)
+    ctx.set_graphs(False)
+    ctx.vbuild(S.xyz, S.types.astype(np.int32), tr, tv, [1024, 1024], S.mins)
+    vmin = ctx.info()["vmin"]
+    dE = 80.0
+    nc = 9
+    an_re, _, zn = sep.coefficients(S.el, nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+    start = sep.start_states(START_SEED, 24, S.ngrid, S.dv)
+    for _ in range(2):
+        out = ctx.filter(start, an_re, zn, 4.0 / dE, vmin)
+    print(json.dumps({"profile_case": args.profile, "states": 24, "newton_steps": nc - 1,
+                      "checksum": float(np.abs(out).sum())}))
+
+
+# ---------------------------------------------------------------------------
+def build_system():
+    from semi_empirical_pseudopotentials_gb300 import systems
+
+    w = WORKLOAD
+    return systems.make_system(w["name"], w["radius_nm"], w["n"], w["ms"], w["ns"], w["nc"],
+                               seed=w["seed"], elmin=w["elmin"], elmax=w["elmax"])
+
+
+def tables(sep, S):
+    """Form factor -> real-space table (pot.c) -> shifted (read.c:105-108)."""
+    tr = np.zeros((2, 1024))
+    tv = np.zeros((2, 1024))
+    for t in (0, 1):
+        r, v = sep.form_factor_table(S.params[t], S.vol_per_atom)
+        tr[t], tv[t] = r, v - v[-1]
+    return tr, tv
+
+
+def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=16):
+    """Compulsory HBM bytes of one launch (c: bytes per complex, r: per real)."""
+    if kind in ("x_fwd", "y_fwd", "z_fki", "y_inv"):
+        return 2 * c * n * npairs                      # read + write the grids
+    if kind == "x_inv_epi_fwd":
+        return (4 * c) * n * npairs + r * n            # T in/out, psi_in, psi_out, V once
+    if kind == "accumulate":
+        return kblock * c * n * npairs + 2 * (2 * ms * r) * n * npairs
+    raise ValueError(kind)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) == 7:
+                self.samples.append(f)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+def cpu_baseline(S, pot, dE, an_re, zn, vmin, seconds=12.0):
+    """The oracle's filter cycles on the host cores (bounded sample)."""
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    n = S.ngrid
+    ks = O.ksqr(*S.dims, *S.steps)
+    octx = O.Context(S.dims, pot, ks, S.dv)
+    ns = cores
+    start = O.start_states(START_SEED, ns, n, S.dv)
+    # time a short cycle first, then size the sample to about `seconds`
+    nc = 3
+    _, sec = octx.filter_batch(start, an_re[:, :nc], zn[:nc], 4.0 / dE, vmin, nthreads=cores)
+    per_step = sec / (nc - 1)
+    nc = max(3, min(1024, int(seconds / max(per_step, 1e-6)) + 1))
+    _, sec = octx.filter_batch(start, an_re[:, :nc], zn[:nc], 4.0 / dE, vmin, nthreads=cores)
+    applies = ns * (nc - 1)
+    return {"value": applies / sec, "unit": "applies/s", "cores": cores, "kind": "port",
+            "sample": f"{ns} start states x {nc - 1} Newton steps of the 128^3 workload "
+                      f"({applies} H applies, {sec:.1f} s), oracle C restatement with its own "
+                      "Stockham FFT, OpenMP over start states as filter/main.c:92-98"}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    """--impl reference: the reference's CPU filter (oracle port) on host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import semi_empirical_pseudopotentials_gb300 as sep  # host helpers only
+    from oracle import oracle as O
+
+    S = build_system()
+    tr, tv = tables(sep, S)
+    pot = O.vbuild(*S.xyz.T, S.types, tr, tv, [1024, 1024], S.dims, S.mins, S.steps)
+    vmin = float(pot.min())
+    ks = O.ksqr(*S.dims, *S.steps)
+    octx = O.Context(S.dims, pot, ks, S.dv)
+    dE = 80.0  # fixed spectral width for the timing sample (the coefficients' values do not
+    #            change the cost of a Newton step)
+    nc = 1024
+    an_re, _, zn = sep.coefficients(S.el, nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+    cores = os.cpu_count() or 1
+    ns = cores
+    start = O.start_states(START_SEED, ns, S.ngrid, S.dv)
+    _, sec = octx.filter_batch(start, an_re[:, :3], zn[:3], 4.0 / dE, vmin, nthreads=cores)
+    ncs = max(3, min(1024, int(8.0 / max(sec / 2, 1e-6)) + 1))
+    times = []
+    for i in range(args.warmup + args.steps):
+        _, sec = octx.filter_batch(start, an_re[:, :ncs], zn[:ncs], 4.0 / dE, vmin,
+                                   nthreads=cores)
+        if i >= args.warmup:
+            times.append(sec)
+    applies = ns * (ncs - 1)
+    T = sum(times)
+    value = applies * len(times) / T
+    line = {"impl": "reference", "metric": "Hpsi applies/s at 128^3", "value": value,
+            "unit": "applies/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * T / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "r2.5nm CdSe-like sphere, 128^3, 64 states x 8 targets, "
+                                   "nc 1024", "step": f"{ns} states x {ncs - 1} Newton steps"},
+            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": cores, "kind": "port",
+                             "sample": f"{ns} start states x {ncs - 1} Newton steps per step"},
+            "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_sep(args):
+    import torch
+
+    import semi_empirical_pseudopotentials_gb300 as sep
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    S = build_system()
+    tr, tv = tables(sep, S)
+    n = S.ngrid
+    ns, ms, nc = S.ns, S.ms, S.nc
+    ctx = sep.Context(S.dims, S.steps, precision="mixed")
+    pot = ctx.vbuild(S.xyz, S.types.astype(np.int32), tr, tv, [1024, 1024], S.mins,
+                     install=True)
+    vmin = ctx.info()["vmin"]
+    emax, dE, iters = ctx.energy_range(vmin)
+    dt = (nc / (2.5 * dE)) ** 2
+    an_re, _, zn = sep.coefficients(S.el, nc, dE, vmin, dt)
+    start_h = sep.start_states(START_SEED, ns, n, S.dv)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    start_d = torch.from_numpy(start_h).to(f"cuda:{local}")
+    out_d = torch.empty((ns, ms, n), dtype=torch.float64, device=f"cuda:{local}")
+
+    def step_dev():
+        ctx.filter_dev(start_d.data_ptr(), ns, an_re, zn, 4.0 / dE, vmin, out_d.data_ptr())
+
+    for _ in range(args.warmup):
+        step_dev()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_dev()
+        e1.record(stream)
+        e1.synchronize()
+    barrier()
+    t_dev = e0.elapsed_time(e1) * 1e-3
+    if dist:
+        tt = torch.tensor([t_dev], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    applies_step = ns * (nc - 1)
+    value = world * applies_step * args.steps / t_dev
+
+    # e2e through the host-pointer call, pinned host buffers
+    start_p = torch.from_numpy(start_h).pin_memory()
+    out_p = torch.empty((ns, ms, n), dtype=torch.float64).pin_memory()
+    start_np, out_np = start_p.numpy(), out_p.numpy()
+    ctx.filter(start_np, an_re, zn, 4.0 / dE, vmin, out=out_np)  # warm the host path
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.filter(start_np, an_re, zn, 4.0 / dE, vmin, out=out_np)
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if dist:
+        tt = torch.tensor([t_e2e], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = {"value": world * applies_step * args.steps / t_e2e, "unit": "applies/s",
+           "h2d_bytes_per_step": int(start_h.nbytes), "d2h_bytes_per_step": int(ns * ms * n * 8)}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        peaks = measured_peaks()
+        # roofline of the dominant kernel: per-launch device times of each kernel kind
+        names = ["x_fwd", "y_fwd", "z_fki", "y_inv", "x_inv_epi_fwd", "accumulate"]
+        npairs = (ns + 1) // 2
+        per = ctx.time_passes(npairs, reps=10)
+        launches = [1, nc - 1, nc - 1, nc - 1, nc - 1, (nc + 15) // 16]
+        share = [p * l for p, l in zip(per, launches)]
+        k = int(np.argmax(share))
+        byts = algorithmic_bytes(names[k], npairs, n, 8, 4)
+        achieved = byts / (per[k] * 1e-3) / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+        if os.path.exists(tf):
+            with open(tf) as f:
+                traffic = json.load(f).get("mixed_128", {}).get(names[k])
+        extras["roofline"] = {
+            "bound": "hbm", "kernel": names[k], "achieved": achieved,
+            "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+            "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic,
+            "algorithmic_bytes_per_launch": byts,
+            "per_launch_ms": dict(zip(names, [round(p, 4) for p in per])),
+            "time_share": dict(zip(names, [round(s / sum(share), 4) for s in share])),
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+        # plain FP64 filter on the same workload: a bounded sample of Newton steps
+        ctx64 = sep.Context(S.dims, S.steps, precision="f64")
+        ctx64.vbuild(S.xyz, S.types.astype(np.int32), tr, tv, [1024, 1024], S.mins)
+        ncs = 129
+        ctx64.filter_dev(start_d.data_ptr(), ns, an_re[:, :ncs], zn[:ncs], 4.0 / dE, vmin,
+                         out_d.data_ptr())
+        s64 = torch.cuda.ExternalStream(ctx64.stream())
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(s64)
+        ctx64.filter_dev(start_d.data_ptr(), ns, an_re[:, :ncs], zn[:ncs], 4.0 / dE, vmin,
+                         out_d.data_ptr())
+        f1.record(s64)
+        f1.synchronize()
+        t64 = f0.elapsed_time(f1) * 1e-3
+        per64 = ctx64.time_passes(npairs, reps=3)
+        extras["fp64"] = {"value": ns * (ncs - 1) / t64, "unit": "applies/s",
+                          "sample": f"{ns} states x {ncs - 1} Newton steps",
+                          "per_launch_ms": dict(zip(names, [round(p, 4) for p in per64])),
+                          "note": "complex128 line passes run at the FP64 pipe rate "
+                                  "(about 1.25 TFLOP/s on this part)"}
+        # whole path: energy range -> filter -> ortho -> Rayleigh-Ritz -> sigma
+        del out_d
+        torch.cuda.empty_cache()
+        res = ctx.pipeline(start_h, S.el, nc, vmin)
+        t = res["timing"]
+        ev, sg = res["eval"], res["sigma"]
+        conv = int(np.sum(sg < 1e-5))
+        extras["time_to_band_edge"] = {
+            "precision": "mixed", "seconds": t["total_s"],
+            "stages_s": {k2: round(t[k2], 3) for k2 in ("energy_range_s", "filter_s", "ortho_s",
+                                                         "rayleigh_ritz_s", "sigma_s")},
+            "mkept": res["mkept"], "converged_sigma_1e-5": conv,
+            "window": [float(S.el[0]), float(S.el[-1])]}
+        ctx64.close()
+        extras["cpu_baseline"] = cpu_baseline(S, pot, dE, an_re, zn, vmin)
+
+    if rank == 0:
+        launches_step = 1 + 1 + 4 * (nc - 1) + (nc + 15) // 16 + 1
+        line = {"metric": "Hpsi applies/s at 128^3", "value": value, "unit": "applies/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+                "data": "synthetic",
+                "config": {"workload": "r2.5nm CdSe-like sphere (2317 atoms), 128^3, "
+                                       "64 start states x 8 targets, nc 1024",
+                           "precision": "complex64 filter, FP32 accumulation",
+                           "l2": "inputs larger than L2 (about 13 GB of filter state)",
+                           "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                           "dE": dE, "power_iterations": iters},
+                "e2e": e2e, "gpu_launches": launches_step * args.steps,
+                "clocks": clk.summary()}
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_sep(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,167 @@
+/*
+ * sep_gb300.h -- C ABI of libsep_gb300.so, the GB300 (sm_103a) implementation
+ * of the filter-diagonalisation path of the semi-empirical pseudopotential
+ * method (the reference's filter/ program).
+ *
+ * Plain C types only: host or device pointers plus sizes.  All functions
+ * return an int status (SEP_OK = 0, negative on error) and leave a message for
+ * sep_last_error().  Arrays follow the reference's layouts:
+ *   grids        x fastest, jxyz = nx (ny jz + jy) + jx   (filter/init.c:139-141)
+ *   complex      interleaved {re, im} doubles, as zomplex  (filter/fd.h:17-19)
+ *   state blocks state-major psitot[state * ngrid + g]     (filter/main.c:86)
+ * Host-pointer entry points copy in and out; the *_dev variants take device
+ * pointers and run on the context's stream.
+ *
+ * The fd.h-compatible entry points (same names and arguments as the
+ * reference's filter/fd.h:81-145) are declared in sep_fd_compat.h.
+ */
+#ifndef SEP_GB300_H
+#define SEP_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum sep_status {
+  SEP_OK = 0,
+  SEP_ERR_ARG = -1,          /* bad argument or unsupported size */
+  SEP_ERR_CUDA = -2,         /* CUDA runtime / device error */
+  SEP_ERR_NOMEM = -3,        /* device allocation failed */
+  SEP_ERR_SOLVER = -4,       /* dense eigensolver failed (reference: dsyev/dgesvd info) */
+  SEP_ERR_NO_DEVICE = -5,    /* no CUDA device / library built without one */
+  SEP_ERR_NUMERIC = -6       /* non-finite values, empty subspace */
+};
+
+enum sep_precision {
+  SEP_PREC_F64 = 0,    /* complex128 filter, FP64 subspace */
+  SEP_PREC_MIXED = 1   /* complex64 filter with FP32 accumulation, FP64 subspace */
+};
+
+typedef struct sep_ctx sep_ctx;
+
+/* Stage wall times of sep_pipeline, seconds (CUDA events on the context stream). */
+typedef struct {
+  double energy_range_s, filter_s, ortho_s, rayleigh_ritz_s, sigma_s, total_s;
+  long power_iterations, mkept, h_applies;
+  double emax, dE, dt;
+} sep_timing;
+
+/* ---- library ------------------------------------------------------------ */
+const char *sep_last_error(void);
+int sep_version(void);                      /* 10000*major + 100*minor + patch */
+int sep_device_count(int *count);
+
+/* ---- context: one grid + one local potential -----------------------------
+ * Replaces the grid / ksqr / potl set-up of filter/init.c:90-199 and the FFT
+ * plans of filter/main.c:58-59.  steps = (dx, dy, dz) in bohr; ekinmax = the
+ * kinetic cap in hartree (10.0 in filter/init.c:31; k^2 is pre-scaled by
+ * 1/N and capped at ekinmax/N as filter/init.c:125-143).  potl: N doubles or
+ * NULL (set later).  Supported axis lengths: 16 18 20 24 32 36 40 48 56 64
+ * 72 80 96 112 128 160 192 256. */
+int sep_ctx_create(const long dims[3], const double steps[3], double ekinmax,
+                   const double *potl, int precision, sep_ctx **out);
+int sep_ctx_destroy(sep_ctx *ctx);
+int sep_ctx_set_potential(sep_ctx *ctx, const double *potl);      /* host */
+int sep_ctx_set_potential_dev(sep_ctx *ctx, const double *potl);  /* device */
+/* Vmin, Vmax of the potential (filter/init.c:196-199) and dv = dx dy dz */
+int sep_ctx_info(sep_ctx *ctx, double *vmin, double *vmax, double *dv, long *ngrid);
+int sep_ctx_stream(sep_ctx *ctx, void **cuda_stream);             /* cudaStream_t */
+/* Capture the Newton loop of sep_filter* in a CUDA graph (default 1). */
+int sep_ctx_set_graphs(sep_ctx *ctx, int enable);
+/* Newton steps accumulated per pass over the step history (default 16). */
+int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
+
+/* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------
+ * hpsi = T psi + V psi for nstates complex grids (interleaved complex128). */
+int sep_hamiltonian(sep_ctx *ctx, const double *psi, double *hpsi, long nstates);
+int sep_hamiltonian_dev(sep_ctx *ctx, const double *psi, double *hpsi, long nstates);
+
+/* ---- filter/hnorm.c:11-39 ------------------------------------------------
+ * psin = dE_1 H psim1 - (2 + zm1 + vmin dE_1) psim1 (complex grids). */
+int sep_hnorm(sep_ctx *ctx, const double *psim1, double *psin, long nstates, double dE_1,
+              double vmin, double zm1);
+
+/* ---- Newton filter: filter/filter.c:59-83 (filter) for ns start states ---
+ * start: ns x N real states; an_re: ms x nc (real parts of the reference's
+ * zomplex an[nc*e + j]); zn: nc points; out: ns x ms x N, block s holding
+ * psi0[e][g] = sum_j an_re[e][j] Re psi_j[g] as filter.c computes it.
+ * In SEP_PREC_MIXED the recursion and the sums run in complex64 / FP32. */
+int sep_filter(sep_ctx *ctx, const double *start, long ns, const double *an_re,
+               const double *zn, long ms, long nc, double dE_1, double vmin, double *out);
+int sep_filter_dev(sep_ctx *ctx, const double *start, long ns, const double *an_re,
+                   const double *zn, long ms, long nc, double dE_1, double vmin, double *out);
+
+/* ---- filter/norm.c:40-54 normalize_all, filter/energy.c:28-49 energy_all --- */
+int sep_normalize_all(sep_ctx *ctx, double *psi, long m);
+int sep_energy_all(sep_ctx *ctx, const double *psi, long m, double *ene);
+
+/* ---- filter/energy.c:53-83 get_energy_range ------------------------------
+ * Power iteration from the fixed seed -874917403 until |dE/E| <= 1e-4 or 500
+ * iterations; dE = 1.1 (emax - vmin). */
+int sep_energy_range(sep_ctx *ctx, double vmin, double *emax, double *dE, long *iters);
+
+/* ---- subspace: filter/ortho.c:11-52, filter/Hmat.c:11-86, energy.c:88-119 --
+ * sep_ortho: orthonormalise the m real states in place (dv metric) and keep
+ * the directions whose singular value ratio S_i/S_0 >= 1e-10 as portho does;
+ * *mkept = kept count (the first *mkept rows of psi).
+ * sep_rayleigh_ritz: Hmatreal -- project H, diagonalise, rotate psi in place,
+ * eval ascending.  sep_sigma: sqrt(|<H^2> - <H>^2|) per state. */
+int sep_ortho(sep_ctx *ctx, double *psi, long m, long *mkept);
+int sep_rayleigh_ritz(sep_ctx *ctx, double *psi, long m, double *eval);
+int sep_sigma(sep_ctx *ctx, const double *psi, long m, double *sige);
+
+/* ---- whole path: filter/main.c:64-142 ------------------------------------
+ * start: ns x N real start states (host).  el: ms target energies.  vmin:
+ * minimum of the potential.  dE <= 0: computed by the power iteration.
+ * psi_out (optional, host, ns*ms x N): Ritz vectors, first *mkept rows.
+ * eval / sige: ns*ms entries, first *mkept valid. */
+int sep_pipeline(sep_ctx *ctx, const double *start, long ns, const double *el, long ms,
+                 long nc, double vmin, double dE, double *psi_out, double *eval,
+                 double *sige, long *mkept, sep_timing *timing);
+
+/* ---- host helpers, bit-identical to the reference -----------------------
+ * filter/coeff.c:16-134: Newton coefficients of the Gaussian filters.
+ * an_re, an_im: ms x nc; zn: nc. */
+int sep_coefficients(long ms, long nc, double dE, double vmin, double dt, const double *el,
+                     double *an_re, double *an_im, double *zn);
+/* filter/init.c:236-251 + filter/rand.c:28-66: ns consecutive start states
+ * from one seed (idum <= 0), each normalised with dv; out: ns x ngrid. */
+int sep_start_states(long idum, long ns, long ngrid, double dv, double *out);
+/* filter/init.c:124-144: the capped, 1/N-scaled k^2 grid. */
+int sep_ksqr(const long dims[3], const double steps[3], double ekinmax, double *ksqr);
+/* pseudopotFitting/pot.c:35-63 with hamiltonian.c:91-94: 1024-point
+ * real-space table (r, v) of one species' form factor. */
+int sep_form_factor_table(const double params[4], double vol_per_atom, double *r, double *v);
+
+/* ---- local potential: filter/init.c:157-182 + filter/interpolate.c:11-23 --
+ * potl[g] = sum_a scale_a * table_{type_a}(|r_g - R_a|) on the context grid.
+ * xyz: natom x 3 (centred, bohr); types: natom ints in [0, ntype); scale:
+ * natom (filterStrainCube/interpolate.c:11-25 strain factor) or NULL;
+ * tab_r / tab_v: ntype x tab_stride (shifted tables, filter/read.c:105-108);
+ * tab_n: ntype lengths.  mins = (xmin, ymin, zmin).  The result also becomes
+ * the context's potential when `install` is non-zero. */
+int sep_vbuild(sep_ctx *ctx, long natom, const double *xyz, const int *types,
+               const double *scale, long ntype, const double *tab_r, const double *tab_v,
+               const long *tab_n, long tab_stride, const double mins[3], double *potl,
+               int install);
+/* Backward of sep_vbuild: given dL/dpotl (N doubles), accumulate
+ * dL/dtab_v (ntype x tab_stride) and, when dscale != NULL, dL/dscale (natom). */
+int sep_vbuild_backward(sep_ctx *ctx, long natom, const double *xyz, const int *types,
+                        const double *scale, long ntype, const double *tab_r,
+                        const double *tab_v, const long *tab_n, long tab_stride,
+                        const double mins[3], const double *dpotl, double *dtab_v,
+                        double *dscale);
+
+/* ---- measurement --------------------------------------------------------
+ * Average device time (ms, CUDA events on the context stream) of one launch
+ * of each Newton-step kernel on npairs complex grids in the context's
+ * precision, over reps launches each: ms_out[0..5] = x forward, y forward,
+ * z forward*k^2*inverse, y inverse, x inverse+epilogue+forward, accumulate
+ * (block_steps history grids into ms = 8 state pairs).  No counterpart in the
+ * reference; used for the roofline report. */
+int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -63,6 +63,9 @@ def lib():
                                    C.c_double, dp, dp, dp, dp, C.c_int, C.c_int,
                                    C.POINTER(Timing)]
         L.orc_lapack_load.argtypes = [C.c_char_p]
+        L.orc_filter_batch.restype = C.c_double
+        L.orc_filter_batch.argtypes = [C.c_void_p, C.c_long, dp, dp, dp, C.c_long, C.c_long,
+                                       C.c_double, C.c_double, dp, C.c_int]
         _lib = L
     return _lib
 
@@ -98,6 +101,14 @@ def start_states(idum, ns, ngrid, dv):
     """filter/main.c:82-89: ns consecutive init_psi draws from one seed."""
     r = rng(idum)
     return np.stack([init_psi(r, ngrid, dv) for _ in range(ns)])
+
+
+def normalize_all(psi, dv):
+    """filter/norm.c:40-54 on [m, ngrid] real states (returns a copy)."""
+    psi = np.ascontiguousarray(psi, dtype=np.float64).copy()
+    lib().orc_normalize_all(_p(psi), C.c_double(dv), C.c_long(psi.shape[0]),
+                            C.c_long(psi.shape[1]))
+    return psi
 
 
 # ---- set-up ----------------------------------------------------------------
@@ -213,6 +224,18 @@ class Context:
         lib().orc_filter_cycle(self.h, _p(start), _p(an_re), _p(zn), ms, nc, dE_1, vmin,
                                _p(out))
         return out
+
+    def filter_batch(self, start, an_re, zn, dE_1, vmin, nthreads=0):
+        """filter/main.c:92-98: the cycles of [ns, N] start states on OpenMP
+        threads; returns (out [ns, ms, N], wall seconds)."""
+        start = np.ascontiguousarray(start, dtype=np.float64)
+        an_re = np.ascontiguousarray(an_re, dtype=np.float64)
+        zn = np.ascontiguousarray(zn, dtype=np.float64)
+        ms, nc = an_re.shape
+        out = np.empty((start.shape[0], ms, self.ngrid))
+        sec = lib().orc_filter_batch(self.h, start.shape[0], _p(start), _p(an_re), _p(zn), ms,
+                                     nc, dE_1, vmin, _p(out), nthreads)
+        return out, sec
 
     def energy_all(self, psi0):
         psi0 = np.ascontiguousarray(psi0, dtype=np.float64)

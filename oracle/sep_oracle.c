@@ -554,6 +554,23 @@ void orc_sigma(const orc_ctx *c, const double *psi, long m, double *sige) {
   free(hhz);
 }
 
+/* filter/main.c:92-98: the filter cycles of ns start states, one per OpenMP
+ * thread as the reference runs them; returns the wall time in seconds. */
+double orc_filter_batch(const orc_ctx *c, long ns, const double *start, const double *an_re,
+                        const double *zn, long ms, long nc, double dE_1, double vmin,
+                        double *out, int nthreads) {
+  const long n = c->ngrid;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  double t0 = now_s();
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long s = 0; s < ns; s++)
+    orc_filter_cycle(c, start + (size_t)s * n, an_re, zn, ms, nc, dE_1, vmin,
+                     out + (size_t)s * ms * n);
+  return now_s() - t0;
+}
+
 /* ========================================================================= */
 /* Whole pipeline, filter/main.c:64-142, OpenMP over start states as          */
 /* main.c:92-98.                                                              */

@@ -83,6 +83,11 @@ long orc_portho(double *psi, long ngrid, long m, double *sv_out);
 int orc_hmat(const orc_ctx *c, double *psi, long m, double *eval);
 void orc_sigma(const orc_ctx *c, const double *psi, long m, double *sige);
 
+/* filter/main.c:92-98: ns filter cycles over OpenMP threads; returns seconds */
+double orc_filter_batch(const orc_ctx *c, long ns, const double *start, const double *an_re,
+                        const double *zn, long ms, long nc, double dE_1, double vmin,
+                        double *out, int nthreads);
+
 /* ---- whole pipeline (CPU baseline): filter/main.c:64-142 ----------------- */
 typedef struct {
   double energy_range_s, filter_s, ortho_s, hmat_s, sigma_s;

@@ -1,0 +1,321 @@
+"""ctypes binding of libsep_gb300.so (include/sep_gb300.h).
+
+Arrays are numpy float64 / complex128 in the reference's layouts: grids x
+fastest (filter/init.c:139-141), state blocks state-major
+(psitot[state * ngrid + g], filter/main.c:86), complex interleaved.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsep_gb300.so")
+
+PREC = {"f64": 0, "mixed": 1}
+
+_lib = None
+dp = C.POINTER(C.c_double)
+lp = C.POINTER(C.c_long)
+ip = C.POINTER(C.c_int)
+
+
+class SepError(RuntimeError):
+    """A non-zero status from the C ABI, with sep_last_error()'s message."""
+
+    def __init__(self, status, msg):
+        super().__init__(f"sep status {status}: {msg}")
+        self.status = status
+
+
+class Timing(C.Structure):
+    _fields_ = [("energy_range_s", C.c_double), ("filter_s", C.c_double),
+                ("ortho_s", C.c_double), ("rayleigh_ritz_s", C.c_double),
+                ("sigma_s", C.c_double), ("total_s", C.c_double),
+                ("power_iterations", C.c_long), ("mkept", C.c_long), ("h_applies", C.c_long),
+                ("emax", C.c_double), ("dE", C.c_double), ("dt", C.c_double)]
+
+
+def lib():
+    """Load the native library; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SepError(-5, f"{LIB_PATH} is missing: build it with "
+                               "semi_empirical_pseudopotentials_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        L.sep_last_error.restype = C.c_char_p
+        vp = C.c_void_p
+        L.sep_ctx_create.argtypes = [lp, dp, C.c_double, dp, C.c_int, C.POINTER(vp)]
+        for name in ("sep_ctx_destroy",):
+            getattr(L, name).argtypes = [vp]
+        L.sep_ctx_set_potential.argtypes = [vp, dp]
+        L.sep_ctx_set_potential_dev.argtypes = [vp, vp]
+        L.sep_ctx_info.argtypes = [vp, dp, dp, dp, lp]
+        L.sep_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+        L.sep_ctx_set_graphs.argtypes = [vp, C.c_int]
+        L.sep_ctx_set_block_steps.argtypes = [vp, C.c_int]
+        L.sep_hamiltonian.argtypes = [vp, dp, dp, C.c_long]
+        L.sep_hamiltonian_dev.argtypes = [vp, vp, vp, C.c_long]
+        L.sep_hnorm.argtypes = [vp, dp, dp, C.c_long, C.c_double, C.c_double, C.c_double]
+        L.sep_filter.argtypes = [vp, dp, C.c_long, dp, dp, C.c_long, C.c_long, C.c_double,
+                                 C.c_double, dp]
+        L.sep_filter_dev.argtypes = [vp, vp, C.c_long, dp, dp, C.c_long, C.c_long, C.c_double,
+                                     C.c_double, vp]
+        L.sep_normalize_all.argtypes = [vp, dp, C.c_long]
+        L.sep_energy_all.argtypes = [vp, dp, C.c_long, dp]
+        L.sep_energy_range.argtypes = [vp, C.c_double, dp, dp, lp]
+        L.sep_ortho.argtypes = [vp, dp, C.c_long, lp]
+        L.sep_rayleigh_ritz.argtypes = [vp, dp, C.c_long, dp]
+        L.sep_sigma.argtypes = [vp, dp, C.c_long, dp]
+        L.sep_pipeline.argtypes = [vp, dp, C.c_long, dp, C.c_long, C.c_long, C.c_double,
+                                   C.c_double, dp, dp, dp, lp, C.POINTER(Timing)]
+        L.sep_coefficients.argtypes = [C.c_long, C.c_long, C.c_double, C.c_double, C.c_double,
+                                       dp, dp, dp, dp]
+        L.sep_start_states.argtypes = [C.c_long, C.c_long, C.c_long, C.c_double, dp]
+        L.sep_ksqr.argtypes = [lp, dp, C.c_double, dp]
+        L.sep_form_factor_table.argtypes = [dp, C.c_double, dp, dp]
+        L.sep_vbuild.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, dp, lp, C.c_long, dp,
+                                 dp, C.c_int]
+        L.sep_vbuild_backward.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, dp, lp,
+                                          C.c_long, dp, dp, dp, dp]
+        L.sep_time_passes.argtypes = [vp, C.c_long, C.c_int, dp]
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != 0:
+        raise SepError(status, lib().sep_last_error().decode(errors="replace"))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a):
+    return a.ctypes.data_as(dp)
+
+
+def device_count():
+    n = C.c_int()
+    _check(lib().sep_device_count(C.byref(n)))
+    return n.value
+
+
+# ---- host helpers (bit-identical to the reference) --------------------------
+def coefficients(el, nc, dE, vmin, dt):
+    """filter/coeff.c:16-63 -> (an_re [ms, nc], an_im [ms, nc], zn [nc])."""
+    el = _f64(el)
+    ms = len(el)
+    ar, ai, zn = np.empty((ms, nc)), np.empty((ms, nc)), np.empty(nc)
+    _check(lib().sep_coefficients(ms, nc, dE, vmin, dt, _p(el), _p(ar), _p(ai), _p(zn)))
+    return ar, ai, zn
+
+
+def start_states(idum, ns, ngrid, dv):
+    """filter/main.c:82-89 with init_psi (filter/init.c:236-251): [ns, ngrid]."""
+    out = np.empty((ns, ngrid))
+    _check(lib().sep_start_states(idum, ns, ngrid, dv, _p(out)))
+    return out
+
+
+def ksqr(dims, steps, ekinmax=10.0):
+    dims_a = (C.c_long * 3)(*dims)
+    steps_a = _f64(steps)
+    out = np.empty(int(np.prod(dims)))
+    _check(lib().sep_ksqr(dims_a, _p(steps_a), ekinmax, _p(out)))
+    return out
+
+
+def form_factor_table(params, vol_per_atom):
+    """pseudopotFitting/pot.c:35-63 -> (r[1024], v[1024]) unshifted."""
+    a = _f64(params)
+    r, v = np.empty(1024), np.empty(1024)
+    _check(lib().sep_form_factor_table(_p(a), vol_per_atom, _p(r), _p(v)))
+    return r, v
+
+
+class Context:
+    """One grid and one local potential on the GPU (sep_ctx)."""
+
+    def __init__(self, dims, steps, potl=None, precision="f64", ekinmax=10.0):
+        self.dims = tuple(int(d) for d in dims)
+        self.ngrid = int(np.prod(self.dims))
+        self.steps = tuple(float(s) for s in steps)
+        self.precision = precision
+        h = C.c_void_p()
+        dims_a = (C.c_long * 3)(*self.dims)
+        steps_a = _f64(self.steps)
+        pot = None if potl is None else _f64(potl)
+        _check(lib().sep_ctx_create(dims_a, _p(steps_a), ekinmax,
+                                    None if pot is None else _p(pot), PREC[precision],
+                                    C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.sep_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # -- properties
+    def info(self):
+        vmin, vmax, dv, n = C.c_double(), C.c_double(), C.c_double(), C.c_long()
+        _check(lib().sep_ctx_info(self.h, C.byref(vmin), C.byref(vmax), C.byref(dv),
+                                  C.byref(n)))
+        return {"vmin": vmin.value, "vmax": vmax.value, "dv": dv.value, "ngrid": n.value}
+
+    @property
+    def dv(self):
+        return self.info()["dv"]
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(lib().sep_ctx_stream(self.h, C.byref(s)))
+        return s.value
+
+    def set_potential(self, potl):
+        pot = _f64(potl)
+        _check(lib().sep_ctx_set_potential(self.h, _p(pot)))
+
+    def set_graphs(self, enable):
+        _check(lib().sep_ctx_set_graphs(self.h, 1 if enable else 0))
+
+    def set_block_steps(self, k):
+        _check(lib().sep_ctx_set_block_steps(self.h, int(k)))
+
+    # -- stages
+    def hamiltonian(self, psi):
+        """filter/hamiltonian.c:11-23 on complex grids [m, N] (or [N])."""
+        z = np.ascontiguousarray(psi, dtype=np.complex128)
+        shape = z.shape
+        z = z.reshape(-1, self.ngrid)
+        out = np.empty_like(z)
+        _check(lib().sep_hamiltonian(self.h, z.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                                     z.shape[0]))
+        return out.reshape(shape)
+
+    def hnorm(self, psim1, dE_1, vmin, zm1):
+        z = np.ascontiguousarray(psim1, dtype=np.complex128)
+        shape = z.shape
+        z = z.reshape(-1, self.ngrid)
+        out = np.empty_like(z)
+        _check(lib().sep_hnorm(self.h, z.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                               z.shape[0], dE_1, vmin, zm1))
+        return out.reshape(shape)
+
+    def filter(self, start, an_re, zn, dE_1, vmin, out=None):
+        """filter/filter.c:59-83 for [ns, N] start states -> [ns, ms, N]."""
+        start = _f64(start).reshape(-1, self.ngrid)
+        an_re = _f64(an_re)
+        ms, nc = an_re.shape
+        zn = _f64(zn)
+        if out is None:
+            out = np.empty((start.shape[0], ms, self.ngrid))
+        elif (out.dtype != np.float64 or not out.flags.c_contiguous or
+              out.size != start.shape[0] * ms * self.ngrid):
+            raise ValueError("out must be a C-contiguous float64 array of ns*ms*ngrid")
+        _check(lib().sep_filter(self.h, _p(start), start.shape[0], _p(an_re), _p(zn), ms, nc,
+                                dE_1, vmin, _p(out)))
+        return out
+
+    def filter_dev(self, start_ptr, ns, an_re, zn, dE_1, vmin, out_ptr):
+        """Device-pointer variant (start: ns x N, out: ns x ms x N, float64)."""
+        an_re = _f64(an_re)
+        ms, nc = an_re.shape
+        zn = _f64(zn)
+        _check(lib().sep_filter_dev(self.h, C.c_void_p(start_ptr), ns, _p(an_re), _p(zn), ms,
+                                    nc, dE_1, vmin, C.c_void_p(out_ptr)))
+
+    def normalize_all(self, psi):
+        psi = _f64(psi).copy()
+        _check(lib().sep_normalize_all(self.h, _p(psi), psi.shape[0]))
+        return psi
+
+    def energy_all(self, psi):
+        psi = _f64(psi)
+        ene = np.empty(psi.shape[0])
+        _check(lib().sep_energy_all(self.h, _p(psi), psi.shape[0], _p(ene)))
+        return ene
+
+    def energy_range(self, vmin):
+        emax, dE, it = C.c_double(), C.c_double(), C.c_long()
+        _check(lib().sep_energy_range(self.h, vmin, C.byref(emax), C.byref(dE), C.byref(it)))
+        return emax.value, dE.value, it.value
+
+    def ortho(self, psi):
+        psi = _f64(psi).copy()
+        k = C.c_long()
+        _check(lib().sep_ortho(self.h, _p(psi), psi.shape[0], C.byref(k)))
+        return psi[:k.value], k.value
+
+    def rayleigh_ritz(self, psi):
+        psi = _f64(psi).copy()
+        ev = np.empty(psi.shape[0])
+        _check(lib().sep_rayleigh_ritz(self.h, _p(psi), psi.shape[0], _p(ev)))
+        return psi, ev
+
+    def sigma(self, psi):
+        psi = _f64(psi)
+        s = np.empty(psi.shape[0])
+        _check(lib().sep_sigma(self.h, _p(psi), psi.shape[0], _p(s)))
+        return s
+
+    def pipeline(self, start, el, nc, vmin, dE=0.0, want_psi=False):
+        """filter/main.c:64-142 from given start states."""
+        start = _f64(start).reshape(-1, self.ngrid)
+        el = _f64(el)
+        ns, ms = start.shape[0], len(el)
+        m = ns * ms
+        ev, sg = np.zeros(m), np.zeros(m)
+        psi = np.empty((m, self.ngrid)) if want_psi else None
+        k = C.c_long()
+        t = Timing()
+        _check(lib().sep_pipeline(self.h, _p(start), ns, _p(el), ms, nc, vmin, dE,
+                                  None if psi is None else _p(psi), _p(ev), _p(sg),
+                                  C.byref(k), C.byref(t)))
+        kk = k.value
+        return {"eval": ev[:kk], "sigma": sg[:kk], "mkept": kk,
+                "psi": None if psi is None else psi[:kk],
+                "timing": {f: getattr(t, f) for f, _ in Timing._fields_}}
+
+    def time_passes(self, npairs, reps=10):
+        """Average ms per launch: x fwd, y fwd, z fwd*k*inv, y inv, x inv+epi+fwd, accumulate."""
+        out = np.zeros(6)
+        _check(lib().sep_time_passes(self.h, npairs, reps, _p(out)))
+        return out
+
+    def vbuild(self, xyz, types, tab_r, tab_v, tab_n, mins, scale=None, install=True):
+        """filter/init.c:157-182 on this grid; tables [ntype, stride] (shifted)."""
+        xyz = _f64(xyz)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        tab_r, tab_v = _f64(tab_r), _f64(tab_v)
+        tab_n = np.ascontiguousarray(tab_n, dtype=np.int64)
+        sc = None if scale is None else _f64(scale)
+        mins = _f64(mins)
+        out = np.empty(self.ngrid)
+        _check(lib().sep_vbuild(self.h, len(xyz), _p(xyz), types.ctypes.data_as(ip),
+                                None if sc is None else _p(sc), tab_r.shape[0], _p(tab_r),
+                                _p(tab_v), tab_n.ctypes.data_as(lp), tab_r.shape[1], _p(mins),
+                                _p(out), 1 if install else 0))
+        return out
+
+    def vbuild_backward(self, xyz, types, tab_r, tab_v, tab_n, mins, dpotl, scale=None):
+        xyz = _f64(xyz)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        tab_r, tab_v = _f64(tab_r), _f64(tab_v)
+        tab_n = np.ascontiguousarray(tab_n, dtype=np.int64)
+        sc = None if scale is None else _f64(scale)
+        mins = _f64(mins)
+        g = _f64(dpotl)
+        dtab = np.zeros_like(tab_v)
+        dsc = None if sc is None else np.zeros(len(xyz))
+        _check(lib().sep_vbuild_backward(self.h, len(xyz), _p(xyz), types.ctypes.data_as(ip),
+                                         None if sc is None else _p(sc), tab_r.shape[0],
+                                         _p(tab_r), _p(tab_v), tab_n.ctypes.data_as(lp),
+                                         tab_r.shape[1], _p(mins), _p(g), _p(dtab),
+                                         None if dsc is None else _p(dsc)))
+        return dtab, dsc

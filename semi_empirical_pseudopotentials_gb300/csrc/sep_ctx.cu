@@ -1,0 +1,638 @@
+// sep_ctx.cu -- orchestration of the filter path on one GPU.
+//
+// Stage order and semantics follow filter/main.c:64-142; every stage runs on
+// the context's stream with device-resident data:
+//   energy range (power iteration)  -> Newton filter (graph-captured loop)
+//   -> normalise -> ortho (Gram + eigensolver, two passes) -> Rayleigh-Ritz
+//   -> sigma.
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "sep_ctx.cuh"
+
+namespace sep {
+
+namespace {
+thread_local std::string g_err;
+}
+
+void set_error(const std::string& msg) { g_err = msg; }
+const char* last_error() { return g_err.c_str(); }
+
+int cuda_fail(cudaError_t e, const char* what, int line) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "CUDA error %d (%s) at sep_ctx.cu:%d in %s", (int)e,
+           cudaGetErrorString(e), line, what);
+  set_error(buf);
+  return (e == cudaErrorMemoryAllocation) ? kErrNomem : kErrCuda;
+}
+int arg_fail(const char* msg) {
+  set_error(msg);
+  return kErrArg;
+}
+
+#define CK(...)                                              \
+  do {                                                        \
+    cudaError_t _e = (__VA_ARGS__);                                  \
+    if (_e != cudaSuccess) return cuda_fail(_e, #__VA_ARGS__, __LINE__); \
+  } while (0)
+#define CKS(...)                                                          \
+  do {                                                                     \
+    cusolverStatus_t _s = (__VA_ARGS__);                                          \
+    if (_s != CUSOLVER_STATUS_SUCCESS) {                                   \
+      char _b[256];                                                        \
+      snprintf(_b, sizeof _b, "cusolver status %d at sep_ctx.cu:%d in %s", \
+               (int)_s, __LINE__, #__VA_ARGS__);                                  \
+      set_error(_b);                                                       \
+      return kErrSolver;                                                   \
+    }                                                                      \
+  } while (0)
+#define RET(...)               \
+  do {                       \
+    int _r = (__VA_ARGS__);            \
+    if (_r != kOk) return _r; \
+  } while (0)
+
+cudaError_t DevBuf::ensure(size_t want) {
+  if (want <= bytes) return cudaSuccess;
+  release();
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    bytes = 0;
+    return e;
+  }
+  bytes = want;
+  return cudaSuccess;
+}
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+bool length_supported(int L) {
+  static const int ok[] = {16, 18, 20, 24, 32, 36, 40, 48, 56, 64, 72, 80, 96, 112, 128, 160,
+                           192, 256};
+  for (int v : ok)
+    if (v == L) return true;
+  return false;
+}
+
+namespace {
+
+void drop_graphs(sep_ctx* c) {
+  for (auto& g : c->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+}
+
+// grow a workspace buffer; a reallocation invalidates captured graphs
+int grow(sep_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes <= b.bytes) return kOk;
+  cudaStreamSynchronize(c->stream);
+  drop_graphs(c);
+  cudaError_t e = b.ensure(bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "workspace allocation", __LINE__);
+  return kOk;
+}
+
+size_t free_device_bytes() {
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return 0;
+  return fr;
+}
+
+// ------------------------------------------------------------------------
+// Newton filter, filter/filter.c:59-83, for the pairs of one chunk.
+template <typename T> struct Prec;
+template <> struct Prec<double> {
+  static GridDev<double>& grid(sep_ctx* c) { return c->g64; }
+};
+template <> struct Prec<float> {
+  static GridDev<float>& grid(sep_ctx* c) { return c->g32; }
+};
+
+template <typename T>
+int newton_loop(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K) {
+  GridDev<T>& g = Prec<T>::grid(c);
+  const long long n = c->n;
+  cx<T>* hist = c->w_hist.as<cx<T>>();
+  cx<T>* fft = c->w_fft.as<cx<T>>();
+  T* acc = c->w_acc.as<T>();
+  const T* an = c->w_coef.as<T>();
+  const T* steps = c->w_steps.as<T>();
+  cudaStream_t s = c->stream;
+  PassIO<T> io;
+  io.data = fft;
+  io.src = hist;  // slot 0 = the start states
+  CK(run_pass<T>(0, kFwd, g, io, Bc, s));
+  io.src = nullptr;
+  io.coefs = steps;
+  for (long j = 1; j < nc; ++j) {
+    CK(run_pass<T>(1, kFwd, g, io, Bc, s));
+    CK(run_pass<T>(2, kFwdKInv, g, io, Bc, s));
+    CK(run_pass<T>(1, kInv, g, io, Bc, s));
+    io.psi_in = hist + (long long)((j - 1) % K) * Bc * n;
+    io.psi_out = hist + (long long)(j % K) * Bc * n;
+    io.step = (int)j;
+    CK(run_pass<T>(0, (j + 1 < nc) ? kInvEpiFwd : kInvEpi, g, io, Bc, s));
+    if ((j + 1) % K == 0 || j == nc - 1) {
+      const long count = j % K + 1;
+      const long j0 = j - count + 1;
+      CK(newton_accumulate<T, T>(hist, K, Bc, n, j0, (int)count, an, nc, (int)ms, acc, nstates,
+                                 j0 == 0, s));
+    }
+  }
+  if (nc == 1)
+    CK(newton_accumulate<T, T>(hist, K, Bc, n, 0, 1, an, nc, (int)ms, acc, nstates, true, s));
+  return kOk;
+}
+
+template <typename T>
+int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
+                const double* zn, long ms, long nc, double dE_1, double vmin, double* d_out) {
+  const long long n = c->n;
+  int K = c->block_steps;
+  if (K > nc) K = (int)nc;
+  if (K < 1) K = 1;
+  const long long B = (ns + 1) / 2;
+  const size_t per_pair = sizeof(cx<T>) * (size_t)n * (size_t)(K + 1) +
+                          sizeof(T) * 2 * (size_t)ms * (size_t)n;
+  const size_t have = c->w_hist.bytes + c->w_fft.bytes + c->w_acc.bytes;
+  size_t budget = (size_t)(0.6 * (double)free_device_bytes()) + have;
+  long long Bc = (long long)(budget / per_pair);
+  if (Bc < 1) return arg_fail("filter: not enough device memory for one pair of states");
+  if (Bc > B) Bc = B;
+  if (Bc > 65535) Bc = 65535;
+  RET(grow(c, c->w_hist, sizeof(cx<T>) * (size_t)n * K * Bc));
+  RET(grow(c, c->w_fft, sizeof(cx<T>) * (size_t)n * Bc));
+  RET(grow(c, c->w_acc, sizeof(T) * 2 * (size_t)ms * n * Bc));
+  RET(grow(c, c->w_coef, sizeof(T) * (size_t)ms * nc));
+  RET(grow(c, c->w_steps, sizeof(T) * 2 * (size_t)nc));
+  // coefficients and per-step epilogue scalars (hnorm.c:17-23)
+  {
+    std::vector<T> a((size_t)ms * nc), st(2 * (size_t)nc, T(0));
+    for (size_t i = 0; i < a.size(); ++i) a[i] = (T)an_re[i];
+    for (long j = 1; j < nc; ++j) {
+      const double shift = 2.0 + zn[j - 1] + vmin * dE_1;
+      st[2 * j] = (T)dE_1;
+      st[2 * j + 1] = (T)(-shift);
+    }
+    CK(cudaMemcpyAsync(c->w_coef.p, a.data(), sizeof(T) * a.size(), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemcpyAsync(c->w_steps.p, st.data(), sizeof(T) * st.size(), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+  }
+  for (long long b0 = 0; b0 < B; b0 += Bc) {
+    const int bc = (int)std::min<long long>(Bc, B - b0);
+    const long long s0 = 2 * b0;
+    const long long nst = std::min<long long>(2LL * bc, ns - s0);
+    CK(pack_pairs<T, double>(d_start + s0 * n, nst, n, c->w_hist.as<cx<T>>(), c->stream));
+    if (c->use_graphs) {
+      const long long key[8] = {bc, nst, ms, nc, K, (long long)(size_t)c->w_hist.p,
+                                (long long)(size_t)c->w_acc.p, (long long)sizeof(T)};
+      FilterGraph* hit = nullptr;
+      for (auto& fg : c->graphs)
+        if (std::memcmp(fg.key, key, sizeof key) == 0) hit = &fg;
+      if (!hit) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int r = newton_loop<T>(c, bc, nst, ms, nc, K);
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &graph);
+        if (r != kOk) return r;
+        CK(e2);
+        FilterGraph fg;
+        std::memcpy(fg.key, key, sizeof key);
+        cudaError_t e3 = cudaGraphInstantiate(&fg.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(e3);
+        if (c->graphs.size() >= 4) {
+          cudaGraphExecDestroy(c->graphs.front().exec);
+          c->graphs.erase(c->graphs.begin());
+        }
+        c->graphs.push_back(fg);
+        hit = &c->graphs.back();
+      }
+      CK(cudaGraphLaunch(hit->exec, c->stream));
+    } else {
+      RET(newton_loop<T>(c, bc, nst, ms, nc, K));
+    }
+    double* dst = d_out + s0 * ms * n;
+    if (sizeof(T) == sizeof(double)) {
+      CK(cudaMemcpyAsync(dst, c->w_acc.p, sizeof(double) * (size_t)nst * ms * n,
+                         cudaMemcpyDeviceToDevice, c->stream));
+    } else {
+      CK(convert_f32_to_f64(c->w_acc.as<float>(), dst, nst * ms * n, c->stream));
+    }
+  }
+  return kOk;
+}
+
+// complex states through H in chunks that fit the scratch
+int apply_h_chunked(sep_ctx* c, const cx<double>* in, cx<double>* out, long long nst) {
+  const long long n = c->n;
+  long long chunk = (long long)((0.25 * (double)free_device_bytes() + c->w_fft.bytes) /
+                                (sizeof(cx<double>) * (double)n));
+  if (chunk < 1) return arg_fail("hamiltonian: not enough device memory");
+  chunk = std::min<long long>(chunk, std::min<long long>(nst, 4096));
+  RET(grow(c, c->w_fft, sizeof(cx<double>) * (size_t)n * chunk));
+  for (long long b0 = 0; b0 < nst; b0 += chunk) {
+    const int bc = (int)std::min<long long>(chunk, nst - b0);
+    CK(apply_h<double>(c->g64, in + b0 * n, out + b0 * n, c->w_fft.as<cx<double>>(), bc, 1.0,
+                       0.0, c->stream));
+  }
+  return kOk;
+}
+
+// H applied to m real states (rows of psi) -> hpsi rows, via pair packing
+int apply_h_real(sep_ctx* c, const double* d_psi, double* d_hpsi, long long m) {
+  const long long n = c->n;
+  const long long B = (m + 1) / 2;
+  RET(grow(c, c->w_states, sizeof(cx<double>) * (size_t)n * B));
+  RET(grow(c, c->w_states2, sizeof(cx<double>) * (size_t)n * B));
+  CK(pack_pairs<double, double>(d_psi, m, n, c->w_states.as<cx<double>>(), c->stream));
+  RET(apply_h_chunked(c, c->w_states.as<cx<double>>(), c->w_states2.as<cx<double>>(), B));
+  CK(unpack_pairs<double, double>(c->w_states2.as<cx<double>>(), m, n, d_hpsi, c->stream));
+  return kOk;
+}
+
+// symmetric eigen-decomposition in place (column-major == row-major); w ascending
+int syevd(sep_ctx* c, double* d_a, long long m, double* d_w) {
+  int lwork = 0;
+  CKS(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER,
+                                  (int)m, d_a, (int)m, d_w, &lwork));
+  RET(grow(c, c->w_solver, sizeof(double) * ((size_t)lwork + 8)));
+  int* info = reinterpret_cast<int*>(c->w_solver.as<double>() + lwork);
+  CKS(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, (int)m, d_a,
+                       (int)m, d_w, c->w_solver.as<double>(), lwork, info));
+  int hinfo = 0;
+  CK(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (hinfo != 0) {
+    char b[128];
+    snprintf(b, sizeof b, "eigensolver failed, info = %d", hinfo);
+    set_error(b);
+    return kErrSolver;
+  }
+  return kOk;
+}
+
+// rows of psi (m x n) <- W (k x m) psi, in place over column chunks
+int rotate_rows(sep_ctx* c, double* d_psi, long long m, long long k, const double* d_w) {
+  const long long n = c->n;
+  long long cols = (long long)((size_t)1 << 27) / (sizeof(double) * std::max<long long>(k, 1));
+  cols = std::max<long long>(64, std::min<long long>(cols, n));
+  RET(grow(c, c->w_tmp, sizeof(double) * (size_t)k * cols));
+  // psi is row-major m x n; a column chunk is a strided sub-matrix: use a
+  // gather through the temporary (rows of the chunk are contiguous pieces)
+  for (long long g0 = 0; g0 < n; g0 += cols) {
+    const long long w = std::min<long long>(cols, n - g0);
+    // out_chunk (k x w) = W (k x m) * psi[:, g0:g0+w] (m x w, leading dim n)
+    CK(gemm_nn_f64_ld(d_w, d_psi + g0, k, w, m, n, c->w_tmp.as<double>(), c->stream));
+    CK(cudaMemcpy2DAsync(d_psi + g0, sizeof(double) * n, c->w_tmp.p, sizeof(double) * w,
+                         sizeof(double) * w, k, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  return kOk;
+}
+
+}  // namespace
+
+// =========================================================================
+int filter_device(sep_ctx* c, const double* d_start, long ns, const double* an_re,
+                  const double* zn, long ms, long nc, double dE_1, double vmin,
+                  double* d_out) {
+  if (ns < 1 || ms < 1 || nc < 1 || ms > 32) return arg_fail("filter: need ns, nc >= 1 and 1 <= ms <= 32");
+  if (c->precision == 1)
+    return filter_impl<float>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out);
+  return filter_impl<double>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out);
+}
+
+int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nstates) {
+  if (nstates < 1) return arg_fail("hamiltonian: nstates < 1");
+  return apply_h_chunked(c, reinterpret_cast<const cx<double>*>(d_psi),
+                         reinterpret_cast<cx<double>*>(d_hpsi), nstates);
+}
+
+int normalize_device(sep_ctx* c, double* d_psi, long m) {
+  RET(grow(c, c->w_red, sizeof(double) * (reduce_partial_doubles(m) + (size_t)m + 64)));
+  double* part = c->w_red.as<double>();
+  CK(normalize_rows<double>(d_psi, m, c->n, c->dv, part, part + reduce_partial_doubles(m),
+                            c->stream));
+  return kOk;
+}
+
+int energy_all_device(sep_ctx* c, const double* d_psi, long m, double* ene_host) {
+  const long long n = c->n;
+  const long long B = (m + 1) / 2;
+  RET(grow(c, c->w_states, sizeof(cx<double>) * (size_t)n * B));
+  RET(grow(c, c->w_states2, sizeof(cx<double>) * (size_t)n * B));
+  RET(grow(c, c->w_red, sizeof(double) * (reduce_partial_doubles(B) + 2 * (size_t)B + 64)));
+  CK(pack_pairs<double, double>(d_psi, m, n, c->w_states.as<cx<double>>(), c->stream));
+  RET(apply_h_chunked(c, c->w_states.as<cx<double>>(), c->w_states2.as<cx<double>>(), B));
+  double* part = c->w_red.as<double>();
+  double2* out = reinterpret_cast<double2*>(part + reduce_partial_doubles(B));
+  CK(pair_dots<double>(c->w_states.as<cx<double>>(), c->w_states2.as<cx<double>>(), (int)B, n,
+                       c->dv, out, part, c->stream));
+  std::vector<double2> h(B);
+  CK(cudaMemcpyAsync(h.data(), out, sizeof(double2) * B, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (long long b = 0; b < B; ++b) {
+    ene_host[2 * b] = h[b].x;
+    if (2 * b + 1 < m) ene_host[2 * b + 1] = h[b].y;
+  }
+  return kOk;
+}
+
+// filter/energy.c:53-83.  The reference applies H twice per iteration; the
+// second product (H psi_{k+1}, used for the energy) is the first product of
+// the next iteration, so it is reused.
+int energy_range_device(sep_ctx* c, double vmin, double* emax, double* dE, long* iters) {
+  const long long n = c->n;
+  std::vector<double> re(n);
+  host::Rand r(-874917403);
+  host::init_psi(r, n, c->dv, re.data());
+  RET(grow(c, c->w_states, sizeof(cx<double>) * (size_t)n));
+  RET(grow(c, c->w_states2, sizeof(cx<double>) * (size_t)n));
+  RET(grow(c, c->w_red, sizeof(double) * (reduce_partial_doubles(1) + 64)));
+  RET(grow(c, c->w_tmp, sizeof(double) * (size_t)n));
+  CK(cudaMemcpyAsync(c->w_tmp.p, re.data(), sizeof(double) * n, cudaMemcpyHostToDevice,
+                     c->stream));
+  cx<double>* psi = c->w_states.as<cx<double>>();
+  cx<double>* hp = c->w_states2.as<cx<double>>();
+  CK(pack_pairs<double, double>(c->w_tmp.as<double>(), 1, n, psi, c->stream));
+  double* part = c->w_red.as<double>();
+  double2* d2 = reinterpret_cast<double2*>(part + reduce_partial_doubles(1));
+  double ene = 0.0 + 0.1, old = 0.0;
+  long it = 0;
+  RET(apply_h_chunked(c, psi, hp, 1));  // H psi_0
+  for (it = 0; std::fabs((ene - old) / ene) > 1.0e-4 && it < 500; ++it) {
+    // psi <- H psi / |H psi| (normalize of norm.c:9-36 over re and im)
+    CK(pair_dots<double>(hp, hp, 1, n, 1.0, d2, part, c->stream));
+    double2 nn;
+    CK(cudaMemcpyAsync(&nn, d2, sizeof nn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const double nrm = std::sqrt((nn.x + nn.y) * c->dv);
+    CK(scale_copy<double>(hp, psi, n, 1.0 / nrm, c->stream));
+    old = ene;
+    RET(apply_h_chunked(c, psi, hp, 1));
+    CK(pair_dots<double>(psi, hp, 1, n, c->dv, d2, part, c->stream));
+    CK(cudaMemcpyAsync(&nn, d2, sizeof nn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    ene = nn.x + nn.y;
+  }
+  *emax = ene;
+  *dE = 1.1 * (ene - vmin);
+  if (iters) *iters = it;
+  if (!std::isfinite(ene)) {
+    set_error("energy range: power iteration produced a non-finite energy");
+    return kErrNumeric;
+  }
+  return kOk;
+}
+
+// filter/ortho.c:11-52: orthonormalise the filtered states (dgesvd "O", in
+// place) and keep the directions with singular-value ratio S_i/S_0 >= 1e-10.
+//
+// Level 1: the dv-weighted Gram matrix G = Psi Psi^T dv has eigenpairs
+// (S_i^2, v_i); Q1 = Lambda^-1/2 V^T Psi are the left singular vectors of the
+// directions G resolves (S_i/S_0 above ~sqrt(m eps), here 2e-7), cleaned by a
+// symmetric (Loewdin) second pass.
+// Level 2: the part of Psi outside span(Q1), R = Psi - Q1^T (Q1 Psi^T dv)
+// (projected twice), has the small singular values as the large ones of its
+// own Gram matrix; its directions down to S/S_0 = 1e-10 are appended the same
+// way.  Rows of psi on return: Q1 then Q2, largest singular values first.
+namespace {
+
+// out (k x n, dense) = W (k x m) * psi (m x n), over column chunks through w_tmp
+int rotate_into(sep_ctx* c, const double* d_psi, long long m, long long k, const double* d_w,
+                double* d_out) {
+  const long long n = c->n;
+  long long cols = (long long)((size_t)1 << 27) / (sizeof(double) * std::max<long long>(k, 1));
+  cols = std::max<long long>(64, std::min<long long>(cols, n));
+  RET(grow(c, c->w_tmp, sizeof(double) * (size_t)k * cols));
+  for (long long g0 = 0; g0 < n; g0 += cols) {
+    const long long w = std::min<long long>(cols, n - g0);
+    CK(gemm_nn_f64_ld(d_w, d_psi + g0, k, w, m, n, c->w_tmp.as<double>(), c->stream));
+    CK(cudaMemcpy2DAsync(d_out + g0, sizeof(double) * n, c->w_tmp.p, sizeof(double) * w,
+                         sizeof(double) * w, k, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  return kOk;
+}
+
+// x (m x n) -= P^T Q with P = Q x^T dv (k x m): removes span(Q) from the rows of x
+int project_out(sep_ctx* c, double* d_x, long long m, const double* d_q, long long k,
+                double* P, double* Pt) {
+  const long long n = c->n;
+  const size_t wd = gemm_nt_work_doubles(k, m, n);
+  RET(grow(c, c->w_gemm, sizeof(double) * wd));
+  CK(gemm_nt_f64(d_q, d_x, k, m, n, c->dv, P, false, c->w_gemm.as<double>(), wd, c->stream));
+  CK(transpose_f64(P, k, m, Pt, c->stream));  // Pt: m x k
+  long long cols = (long long)((size_t)1 << 27) / (sizeof(double) * std::max<long long>(m, 1));
+  cols = std::max<long long>(64, std::min<long long>(cols, n));
+  RET(grow(c, c->w_tmp, sizeof(double) * (size_t)m * cols));
+  for (long long g0 = 0; g0 < n; g0 += cols) {
+    const long long w = std::min<long long>(cols, n - g0);
+    CK(gemm_nn_f64_ld(Pt, d_q + g0, m, w, k, n, c->w_tmp.as<double>(), c->stream));
+    CK(sub_2d_f64(d_x + g0, n, c->w_tmp.as<double>(), m, w, c->stream));
+  }
+  return kOk;
+}
+
+// Loewdin: rows of x (k x n) <- (x x^T dv)^-1/2 x, in place
+int loewdin(sep_ctx* c, double* d_x, long long k, double* G, double* lam, double* W,
+            double* W2) {
+  const long long n = c->n;
+  const size_t wd = gemm_nt_work_doubles(k, k, n);
+  RET(grow(c, c->w_gemm, sizeof(double) * wd));
+  CK(gemm_nt_f64(d_x, d_x, k, k, n, c->dv, G, true, c->w_gemm.as<double>(), wd, c->stream));
+  RET(syevd(c, G, k, lam));
+  // (x x^T dv)^-1/2 = V diag(lam^-1/2) V^T; the column-major eigenvector
+  // buffer read row-major is R = V^T, so the factor is R^T (diag(lam^-1/2) R)
+  CK(scale_rows_isqrt(G, lam, k, W, c->stream));
+  CK(transpose_f64(G, k, k, W2, c->stream));
+  CK(gemm_nn_f64(W2, W, k, k, k, G, c->stream));
+  return rotate_rows(c, d_x, k, k, G);
+}
+
+}  // namespace
+
+int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept) {
+  const long long n = c->n;
+  RET(grow(c, c->w_small, sizeof(double) * (6 * (size_t)m * m + 4 * (size_t)m)));
+  double* G = c->w_small.as<double>();
+  double* lam = G + (size_t)m * m;
+  double* W = lam + m;
+  double* W2 = W + (size_t)m * m;
+  double* P = W2 + (size_t)m * m;
+  double* Pt = P + (size_t)m * m;
+  RET(grow(c, c->w_states2, sizeof(double) * (size_t)n * m));  // Q rows
+  double* Q = c->w_states2.as<double>();
+  const size_t wd = gemm_nt_work_doubles(m, m, n);
+  RET(grow(c, c->w_gemm, sizeof(double) * wd));
+  CK(gemm_nt_f64(d_psi, d_psi, m, m, n, c->dv, G, true, c->w_gemm.as<double>(), wd,
+                 c->stream));
+  RET(syevd(c, G, m, lam));
+  std::vector<double> hl(m);
+  CK(cudaMemcpyAsync(hl.data(), lam, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const double top = hl[m - 1];
+  if (!(top > 0.0) || !std::isfinite(top)) {
+    set_error("ortho: the states are zero or not finite");
+    return kErrNumeric;
+  }
+  const double kRatio = 1.0e-10;                 // filter/ortho.c:41-46
+  const double level1 = 2.0e-7;                  // what one Gram pass resolves
+  long k0 = 0;
+  while (k0 < m && !(std::sqrt(std::max(hl[k0], 0.0) / top) >= level1)) ++k0;
+  const long k1 = m - k0;
+  CK(scale_eigvecs(G, lam, m, k0, W, c->stream));
+  RET(rotate_into(c, d_psi, m, k1, W, Q));
+  RET(loewdin(c, Q, k1, G, lam, W, W2));
+  long k2 = 0;
+  if (k0 > 0) {
+    // level 2 on the remainder of psi
+    RET(project_out(c, d_psi, m, Q, k1, P, Pt));
+    RET(project_out(c, d_psi, m, Q, k1, P, Pt));
+    CK(gemm_nt_f64(d_psi, d_psi, m, m, n, c->dv, G, true, c->w_gemm.as<double>(), wd,
+                   c->stream));
+    RET(syevd(c, G, m, lam));
+    CK(cudaMemcpyAsync(hl.data(), lam, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // at most k0 new directions, each with S/S_0 >= 1e-10
+    long r0 = m;
+    while (r0 > 0 && m - r0 < k0 && std::sqrt(std::max(hl[r0 - 1], 0.0) / top) >= kRatio) --r0;
+    k2 = m - r0;
+    if (k2 > 0) {
+      CK(scale_eigvecs(G, lam, m, r0, W, c->stream));
+      RET(rotate_into(c, d_psi, m, k2, W, Q + (size_t)k1 * n));
+      double* Q2 = Q + (size_t)k1 * n;
+      RET(project_out(c, Q2, k2, Q, k1, P, Pt));
+      RET(loewdin(c, Q2, k2, G, lam, W, W2));
+    }
+  }
+  const long k = k1 + k2;
+  CK(cudaMemcpyAsync(d_psi, Q, sizeof(double) * (size_t)n * k, cudaMemcpyDeviceToDevice,
+                     c->stream));
+  *mkept = k;
+  return kOk;
+}
+
+// filter/Hmat.c:11-86: H_ij = <H psi_i | psi_j> dv over the kept states, the
+// symmetric part diagonalised, psi rotated onto the eigenvectors.
+int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host) {
+  const long long n = c->n;
+  RET(grow(c, c->w_small, sizeof(double) * (4 * (size_t)m * m + 4 * (size_t)m)));
+  double* A = c->w_small.as<double>();
+  double* lam = A + (size_t)m * m;
+  double* At = lam + m;
+  // H psi for chunks of states, rows of A accumulated chunk by chunk
+  long long chunk = std::min<long long>(m, 256);
+  RET(grow(c, c->w_hpsi, sizeof(double) * (size_t)n * chunk));
+  double* hps = c->w_hpsi.as<double>();
+  const size_t wd = gemm_nt_work_doubles(chunk, m, n);
+  RET(grow(c, c->w_gemm, sizeof(double) * wd));
+  for (long long r0 = 0; r0 < m; r0 += chunk) {
+    const long long rc = std::min<long long>(chunk, m - r0);
+    RET(apply_h_real(c, d_psi + r0 * n, hps, rc));
+    CK(gemm_nt_f64(hps, d_psi, rc, m, n, c->dv, A + r0 * m, false, c->w_gemm.as<double>(), wd,
+                   c->stream));
+  }
+  (void)At;
+  CK(symmetrize_f64(A, m, c->stream));
+  RET(syevd(c, A, m, lam));
+  // eigenvector j is column j (A[j*m + i]); new state j = sum_i V[i][j] psi_i
+  // -> rotation matrix rows = columns of V = the col-major buffer read row-major
+  RET(rotate_rows(c, d_psi, m, m, A));
+  CK(cudaMemcpyAsync(eval_host, lam, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return kOk;
+}
+
+// filter/energy.c:88-119: sigma = sqrt(<H^2> - <H>^2) = |H psi - E psi| for a
+// normalised psi (dv metric) with E = <psi|H|psi>.
+int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host) {
+  const long long n = c->n;
+  long long chunk = std::min<long long>(m, 256);
+  RET(grow(c, c->w_hpsi, sizeof(double) * (size_t)n * chunk));
+  RET(grow(c, c->w_red, sizeof(double) * (reduce_partial_doubles(chunk) + 2 * (size_t)chunk + 64)));
+  double* hps = c->w_hpsi.as<double>();
+  double* part = c->w_red.as<double>();
+  double* e = part + reduce_partial_doubles(chunk);
+  double* sg = e + chunk;
+  for (long long r0 = 0; r0 < m; r0 += chunk) {
+    const long long rc = std::min<long long>(chunk, m - r0);
+    RET(apply_h_real(c, d_psi + r0 * n, hps, rc));
+    CK(row_dots<double>(d_psi + r0 * n, hps, rc, n, c->dv, e, part, c->stream));
+    CK(residual_norms(d_psi + r0 * n, hps, e, rc, n, c->dv, sg, part, c->stream));
+    CK(cudaMemcpyAsync(sige_host + r0, sg, sizeof(double) * rc, cudaMemcpyDeviceToHost,
+                       c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return kOk;
+}
+
+template <typename T> int time_passes_impl(sep_ctx* c, long npairs, int reps, double* ms_out) {
+  GridDev<T>& g = Prec<T>::grid(c);
+  const long long n = c->n;
+  const int K = c->block_steps;
+  const int ms = 8;
+  RET(grow(c, c->w_hist, sizeof(cx<T>) * (size_t)n * K * npairs));
+  RET(grow(c, c->w_fft, sizeof(cx<T>) * (size_t)n * npairs));
+  RET(grow(c, c->w_acc, sizeof(T) * 2 * (size_t)ms * n * npairs));
+  RET(grow(c, c->w_coef, sizeof(T) * (size_t)ms * K));
+  CK(cudaMemsetAsync(c->w_hist.p, 0, c->w_hist.bytes, c->stream));
+  CK(cudaMemsetAsync(c->w_fft.p, 0, c->w_fft.bytes, c->stream));
+  CK(cudaMemsetAsync(c->w_coef.p, 0, c->w_coef.bytes, c->stream));
+  cx<T>* hist = c->w_hist.as<cx<T>>();
+  PassIO<T> io;
+  io.data = c->w_fft.as<cx<T>>();
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int axis[5] = {0, 1, 2, 1, 0};
+  const int mode[5] = {kFwd, kFwd, kFwdKInv, kInv, kInvEpiFwd};
+  for (int k = 0; k < 6; ++k) {
+    for (int r = -1; r < reps; ++r) {  // r = -1: warm-up
+      if (r == 0) CK(cudaEventRecord(e0, c->stream));
+      if (k < 5) {
+        PassIO<T> p = io;
+        if (k == 0) p.src = hist;
+        if (k == 4) {
+          p.psi_in = hist;
+          p.psi_out = hist + (long long)n * npairs;
+          p.alpha = T(0.1);
+          p.beta = T(-0.5);
+        }
+        CK(run_pass<T>(axis[k], mode[k], g, p, (int)npairs, c->stream));
+      } else {
+        CK(newton_accumulate<T, T>(hist, K, (int)npairs, n, 0, K, c->w_coef.as<T>(), K, ms,
+                                   c->w_acc.as<T>(), 2 * npairs, false, c->stream));
+      }
+    }
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    ms_out[k] = (double)t / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return kOk;
+}
+
+int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out) {
+  if (npairs < 1 || reps < 1 || c->block_steps < 2)
+    return arg_fail("sep_time_passes: npairs, reps >= 1 and block steps >= 2");
+  if (c->precision == 1) return time_passes_impl<float>(c, npairs, reps, ms_out);
+  return time_passes_impl<double>(c, npairs, reps, ms_out);
+}
+
+}  // namespace sep

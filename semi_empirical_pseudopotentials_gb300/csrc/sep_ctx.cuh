@@ -1,0 +1,76 @@
+// sep_ctx.cuh -- the context behind the C ABI: device tables, workspace,
+// stream, solver handle, cached Newton-loop graphs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sep_engine.cuh"
+#include "sep_host.h"
+#include "sep_kernels.cuh"
+
+namespace sep {
+
+// status codes of include/sep_gb300.h
+enum : int { kOk = 0, kErrArg = -1, kErrCuda = -2, kErrNomem = -3, kErrSolver = -4,
+             kErrNoDevice = -5, kErrNumeric = -6 };
+
+void set_error(const std::string& msg);
+
+// a growable device buffer
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want);
+  void release();
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct FilterGraph {
+  cudaGraphExec_t exec = nullptr;
+  long long key[8] = {};
+};
+
+}  // namespace sep
+
+struct sep_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cusolverDnHandle_t solver = nullptr;
+  int precision = 0;
+  long nx = 0, ny = 0, nz = 0;
+  long long n = 0;
+  double dx = 0, dy = 0, dz = 0, dv = 0, ekinmax = 10.0;
+  double vmin = 0, vmax = 0;
+  bool have_pot = false;
+  bool use_graphs = true;
+  int block_steps = 16;
+  sep::host::KTables ktab;
+  sep::GridDev<double> g64;
+  sep::GridDev<float> g32;
+  // workspace
+  sep::DevBuf w_hist, w_fft, w_acc, w_coef, w_steps, w_start, w_out, w_red, w_small,
+      w_states, w_states2, w_tmp, w_solver, w_gemm, w_hpsi;
+  std::vector<sep::FilterGraph> graphs;
+  ~sep_ctx();
+};
+
+namespace sep {
+
+// device-side operations used by the ABI (all on ctx->stream)
+int filter_device(sep_ctx* c, const double* d_start, long ns, const double* an_re,
+                  const double* zn, long ms, long nc, double dE_1, double vmin, double* d_out);
+int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nstates);
+int energy_all_device(sep_ctx* c, const double* d_psi, long m, double* ene_host);
+int energy_range_device(sep_ctx* c, double vmin, double* emax, double* dE, long* iters);
+int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept);
+int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host);
+int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host);
+int normalize_device(sep_ctx* c, double* d_psi, long m);
+int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out);
+
+}  // namespace sep

@@ -1,0 +1,55 @@
+// sep_engine.cuh -- device-side building blocks of the filter path.
+//
+// Layout in HBM (one context = one grid + one potential):
+//   complex state batch  [B][nz][ny][nx]  (cx<T>, x fastest)
+//   two real states travel in one complex grid: state 2b in the real part,
+//   state 2b+1 in the imaginary part.  H of filter/hamiltonian.c is a real
+//   operator (real V, even k^2), so H(a + i b) = H a + i H b and one complex
+//   transform applies H to two states.
+//   real state blocks    [M][N] (T), state-major like the reference's psitot
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sep_fftpass.cuh"
+
+namespace sep {
+
+// device tables of one grid in one precision
+template <typename T> struct GridDev {
+  int nx = 0, ny = 0, nz = 0;
+  long long n = 0;
+  cx<T>* tw[3] = {nullptr, nullptr, nullptr};  // x, y, z twiddles
+  T* kx = nullptr;
+  T* ky = nullptr;
+  T* kz = nullptr;
+  T kcap = 0;
+  T* pot = nullptr;
+};
+
+// lengths with a compiled line pass
+bool length_supported(int L);
+
+// buffers and scalars of one pass
+template <typename T> struct PassIO {
+  cx<T>* data = nullptr;
+  const cx<T>* src = nullptr;
+  const cx<T>* psi_in = nullptr;
+  cx<T>* psi_out = nullptr;
+  T alpha = T(1), beta = T(0);
+  const T* coefs = nullptr;  // device (alpha, beta) per step
+  int step = 0;
+};
+
+// One line pass over a batch of B grids (see sep_fftpass.cuh for modes).
+template <typename T>
+cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& io, int B,
+                     cudaStream_t s);
+
+// H (or alpha H + beta) applied to B complex grids: out = alpha (T in + V in) + beta in.
+// scratch: B * n complex.  out may not alias in.
+template <typename T>
+cudaError_t apply_h(const GridDev<T>& g, const cx<T>* in, cx<T>* out, cx<T>* scratch, int B,
+                    T alpha, T beta, cudaStream_t s);
+
+}  // namespace sep

@@ -1,0 +1,100 @@
+// sep_pass_impl.cuh -- instantiation and launch of the line passes for one
+// precision (included by sep_pass_f64.cu and sep_pass_f32.cu with SEP_T set).
+#pragma once
+
+#include "sep_engine.cuh"
+
+namespace sep {
+
+namespace {
+
+template <typename T, int L, int AXIS, int MODE>
+cudaError_t launch_one(const PassArgs<T>& a, int B, cudaStream_t s) {
+  constexpr int TL = Tile<T, L, AXIS>::tl;
+  constexpr int NT = Tile<T, L, AXIS>::nt;
+  dim3 grid;
+  if (AXIS == 0) {
+    long long blocks = (a.nbatch_lines + TL - 1) / TL;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    grid = dim3((unsigned)blocks, 1, 1);
+  } else {
+    const int other = (AXIS == 1) ? a.nz : a.ny;
+    if (other > 65535 || B > 65535) return cudaErrorInvalidValue;
+    grid = dim3((unsigned)((a.nx + TL - 1) / TL), (unsigned)other, (unsigned)B);
+  }
+  line_pass<T, L, AXIS, MODE><<<grid, NT, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, int L>
+cudaError_t launch_len(int axis, int mode, const PassArgs<T>& a, int B, cudaStream_t s) {
+  if (axis == 0) {
+    if (mode == kFwd) return launch_one<T, L, 0, kFwd>(a, B, s);
+    if (mode == kInvEpi) return launch_one<T, L, 0, kInvEpi>(a, B, s);
+    if (mode == kInvEpiFwd) return launch_one<T, L, 0, kInvEpiFwd>(a, B, s);
+  } else if (axis == 1) {
+    if (mode == kFwd) return launch_one<T, L, 1, kFwd>(a, B, s);
+    if (mode == kInv) return launch_one<T, L, 1, kInv>(a, B, s);
+  } else if (axis == 2) {
+    if (mode == kFwdKInv) return launch_one<T, L, 2, kFwdKInv>(a, B, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+template <>
+cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
+                            const PassIO<SEP_T>& io, int B, cudaStream_t s) {
+  PassArgs<SEP_T> a;
+  a.data = io.data;
+  a.src = io.src;
+  a.psi_in = io.psi_in;
+  a.psi_out = io.psi_out;
+  a.coefs = io.coefs;
+  a.step = io.step;
+  a.pot = g.pot;
+  a.tw = g.tw[axis];
+  a.kx = g.kx;
+  a.ky = g.ky;
+  a.kz = g.kz;
+  a.kcap = g.kcap;
+  a.alpha = io.alpha;
+  a.beta = io.beta;
+  a.nbatch_lines = (long long)B * g.ny * g.nz;
+  a.nx = g.nx;
+  a.ny = g.ny;
+  a.nz = g.nz;
+  const int L = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+  switch (L) {
+#define SEP_CASE(LL) \
+  case LL: return launch_len<SEP_T, LL>(axis, mode, a, B, s);
+    SEP_CASE(16) SEP_CASE(18) SEP_CASE(20) SEP_CASE(24) SEP_CASE(32) SEP_CASE(36)
+    SEP_CASE(40) SEP_CASE(48) SEP_CASE(56) SEP_CASE(64) SEP_CASE(72) SEP_CASE(80)
+    SEP_CASE(96) SEP_CASE(112) SEP_CASE(128) SEP_CASE(160) SEP_CASE(192) SEP_CASE(256)
+#undef SEP_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <>
+cudaError_t apply_h<SEP_T>(const GridDev<SEP_T>& g, const cx<SEP_T>* in, cx<SEP_T>* out,
+                           cx<SEP_T>* scratch, int B, SEP_T alpha, SEP_T beta,
+                           cudaStream_t s) {
+  cudaError_t e;
+  PassIO<SEP_T> io;
+  io.data = scratch;
+  io.src = in;
+  if ((e = run_pass<SEP_T>(0, kFwd, g, io, B, s))) return e;
+  io.src = nullptr;
+  if ((e = run_pass<SEP_T>(1, kFwd, g, io, B, s))) return e;
+  if ((e = run_pass<SEP_T>(2, kFwdKInv, g, io, B, s))) return e;
+  if ((e = run_pass<SEP_T>(1, kInv, g, io, B, s))) return e;
+  io.psi_in = in;
+  io.psi_out = out;
+  io.alpha = alpha;
+  io.beta = beta;
+  return run_pass<SEP_T>(0, kInvEpi, g, io, B, s);
+}
+
+}  // namespace sep

@@ -1,0 +1,244 @@
+"""CUDA path against the oracle and the reference's own outputs.
+
+Tolerances (FP64 path): one Hamiltonian apply 1e-12 relative (two different
+FFT algorithms agree to roundoff); filtered states 1e-9 relative; Ritz values
+1e-8 Ha against the same algorithm at equal inputs, 1e-6 Ha against the
+published fixture; coefficients, start states and V(r) bit for bit.
+Mixed path: complex64 recursion, errors stated per test.
+"""
+import numpy as np
+import pytest
+
+import semi_empirical_pseudopotentials_gb300 as sep
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_ctx(g, precision="f64"):
+    dims = tuple(int(v) for v in g["dims"])
+    return sep.Context(dims, (float(g["dx"]), float(g["dy"]), float(g["dz"])), potl=g["potl"],
+                       precision=precision)
+
+
+def _random_system(dims, seed=0):
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(dims))
+    steps = (0.7, 0.65, 0.6)
+    # smooth random potential: a few Gaussian wells and bumps
+    nx, ny, nz = dims
+    x = np.arange(nx) * steps[0]
+    y = np.arange(ny) * steps[1]
+    z = np.arange(nz) * steps[2]
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    v = np.zeros_like(X)
+    for _ in range(6):
+        c = rng.uniform(0, 1, 3) * np.array([x[-1], y[-1], z[-1]])
+        a = rng.uniform(-2, 2)
+        v += a * np.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) / 4.0)
+    return steps, v.reshape(n)
+
+
+def test_hamiltonian_matches_reference_output(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    got = ctx.hamiltonian(g["h_in"])
+    ref = g["h_out"]
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("dims", [(16, 18, 20), (36, 36, 36), (32, 40, 48), (64, 64, 64),
+                                  (56, 72, 80), (96, 112, 128), (128, 128, 128)])
+def test_hamiltonian_matches_oracle(dims):
+    steps, pot = _random_system(dims)
+    n = int(np.prod(dims))
+    ks = O.ksqr(*dims, *steps)
+    octx = O.Context(dims, pot, ks, steps[0] * steps[1] * steps[2])
+    ctx = sep.Context(dims, steps, potl=pot)
+    rng = np.random.default_rng(1)
+    nst = 3 if n <= 300000 else 1
+    psi = rng.standard_normal((nst, n)) + 1j * rng.standard_normal((nst, n))
+    got = ctx.hamiltonian(psi)
+    for s in range(nst):
+        ref = octx.hamiltonian(psi[s])
+        err = np.abs(got[s] - ref).max() / np.abs(ref).max()
+        assert err <= 1e-12, (dims, s, err)
+
+
+def test_hnorm_matches_reference_output(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    got = ctx.hnorm(g["h_in"], 4.0 / float(g["dE"]), float(g["vmin"]), 0.37)
+    ref = g["hnorm_out"]
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_filter_matches_reference_output(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    got = ctx.filter(g["init_psi_seed777"][:1], g["an_128"].real, g["zn_128"],
+                     4.0 / float(g["dE"]), float(g["vmin"]))[0]
+    ref = g["filter_out"]
+    for e in range(ref.shape[0]):
+        assert np.abs(got[e] - ref[e]).max() <= 1e-9 * np.abs(ref[e]).max()
+
+
+@pytest.mark.parametrize("ns,block", [(3, 16), (4, 7), (1, 64)])
+def test_filter_matches_oracle(ns, block):
+    dims = (36, 36, 36)
+    steps, pot = _random_system(dims, seed=2)
+    n = int(np.prod(dims))
+    ks = O.ksqr(*dims, *steps)
+    dv = steps[0] * steps[1] * steps[2]
+    octx = O.Context(dims, pot, ks, dv)
+    emax, dE, _ = octx.energy_range(pot.min())
+    nc, ms = 96, 3
+    dt = (nc / (2.5 * dE)) ** 2
+    el = np.array([-1.0, -0.5, 0.0])
+    ar, ai, zn = O.coefficients(el, nc, dE, pot.min(), dt)
+    start = O.start_states(-4242, ns, n, dv)
+    ctx = sep.Context(dims, steps, potl=pot)
+    ctx.set_block_steps(block)
+    got = ctx.filter(start, ar, zn, 4.0 / dE, pot.min())
+    for s in range(ns):
+        ref = octx.filter_cycle(start[s], ar, zn, 4.0 / dE, pot.min())
+        for e in range(ms):
+            err = np.abs(got[s, e] - ref[e]).max() / np.abs(ref[e]).max()
+            assert err <= 1e-9, (s, e, err)
+
+
+def test_filter_graph_and_direct_launches_agree():
+    dims = (32, 40, 48)
+    steps, pot = _random_system(dims, seed=3)
+    n = int(np.prod(dims))
+    dv = steps[0] * steps[1] * steps[2]
+    ar, ai, zn = sep.coefficients([-0.5, 0.2], 40, 30.0, float(pot.min()), (40 / 75.0) ** 2)
+    start = sep.start_states(-99, 5, n, dv)
+    ctx = sep.Context(dims, steps, potl=pot)
+    ctx.set_graphs(True)
+    a = ctx.filter(start, ar, zn, 4.0 / 30.0, float(pot.min()))
+    b = ctx.filter(start, ar, zn, 4.0 / 30.0, float(pot.min()))  # graph replay
+    ctx.set_graphs(False)
+    c = ctx.filter(start, ar, zn, 4.0 / 30.0, float(pot.min()))
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_filter_mixed_precision_error_is_bounded():
+    dims = (36, 36, 36)
+    steps, pot = _random_system(dims, seed=2)
+    n = int(np.prod(dims))
+    dv = steps[0] * steps[1] * steps[2]
+    ks = O.ksqr(*dims, *steps)
+    octx = O.Context(dims, pot, ks, dv)
+    emax, dE, _ = octx.energy_range(pot.min())
+    nc = 96
+    ar, ai, zn = O.coefficients([-1.0, 0.0], nc, dE, pot.min(), (nc / (2.5 * dE)) ** 2)
+    start = O.start_states(-4242, 2, n, dv)
+    ref = np.stack([octx.filter_cycle(start[s], ar, zn, 4.0 / dE, pot.min()) for s in range(2)])
+    ctx = sep.Context(dims, steps, potl=pot, precision="mixed")
+    got = ctx.filter(start, ar, zn, 4.0 / dE, pot.min())
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    # complex64 recursion over 96 Newton steps: FP32 rounding, amplified mildly
+    assert rel < 1e-4, rel
+
+
+def test_energy_range_matches_reference(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    emax, dE, it = ctx.energy_range(float(g["vmin"]))
+    assert abs(dE - float(g["dE"])) <= 1e-9 * float(g["dE"])
+
+
+def test_energy_all_matches_reference(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    got = ctx.energy_all(g["filter_norm"])
+    assert np.allclose(got, g["energy_all"], rtol=1e-11, atol=1e-11)
+
+
+def test_normalize_all():
+    rng = np.random.default_rng(5)
+    dims = (16, 18, 20)
+    ctx = sep.Context(dims, (0.5, 0.5, 0.5), potl=np.zeros(16 * 18 * 20))
+    x = rng.standard_normal((3, 16 * 18 * 20))
+    got = ctx.normalize_all(x)
+    ref = O.normalize_all(x, 0.125)
+    assert np.allclose(got, ref, rtol=1e-14, atol=0)
+
+
+def test_pipeline_matches_reference_run(golden):
+    """The whole path (filter/main.c) against the reference program's eval.dat."""
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    n = int(np.prod(g["dims"]))
+    start = sep.start_states(int(g["run_seed"]), 4, n, float(g["dv"]))
+    res = ctx.pipeline(start, g["el"], 128, float(g["vmin"]))
+    assert abs(res["timing"]["dE"] - float(g["run_dE"])) <= 1e-9 * float(g["run_dE"])
+    assert res["mkept"] == len(g["run_eval"])
+    assert np.allclose(res["eval"], g["run_eval"], rtol=0, atol=1e-8)
+    assert np.allclose(res["sigma"], g["run_sigma"], rtol=2e-5, atol=1e-7)
+
+
+def test_vbuild_bit_exact(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    xyz = np.stack([g["rx"], g["ry"], g["rz"]], axis=1)
+    tab_v = np.stack([O.shift_table(v) for v in g["tab_v"]])
+    pot = ctx.vbuild(xyz, g["types"], g["tab_r"], tab_v, [1024, 1024],
+                     (float(g["xmin"]), float(g["ymin"]), float(g["zmin"])), install=False)
+    assert np.array_equal(pot, g["potl"])
+
+
+def test_vbuild_backward_is_the_adjoint(golden):
+    g = golden("ref_small.npz")
+    ctx = _small_ctx(g)
+    xyz = np.stack([g["rx"], g["ry"], g["rz"]], axis=1)
+    tab_v = np.stack([O.shift_table(v) for v in g["tab_v"]])
+    mins = (float(g["xmin"]), float(g["ymin"]), float(g["zmin"]))
+    rng = np.random.default_rng(9)
+    w = rng.standard_normal(int(np.prod(g["dims"])))
+    scale = 1.0 + 0.01 * rng.standard_normal(len(xyz))
+    dtab, dsc = ctx.vbuild_backward(xyz, g["types"], g["tab_r"], tab_v, [1024, 1024], mins, w,
+                                    scale=scale)
+    # V is linear in the table values: <w, V(tab + d)> - <w, V(tab)> = <dtab, d>
+    d = rng.standard_normal(tab_v.shape) * 1e-3
+    v0 = ctx.vbuild(xyz, g["types"], g["tab_r"], tab_v, [1024, 1024], mins, scale=scale,
+                    install=False)
+    v1 = ctx.vbuild(xyz, g["types"], g["tab_r"], tab_v + d, [1024, 1024], mins, scale=scale,
+                    install=False)
+    assert abs(w @ (v1 - v0) - np.sum(dtab * d)) <= 1e-9 * abs(np.sum(dtab * d)) + 1e-12
+    # and linear in the per-atom scale
+    ds = rng.standard_normal(len(xyz)) * 1e-3
+    v2 = ctx.vbuild(xyz, g["types"], g["tab_r"], tab_v, [1024, 1024], mins, scale=scale + ds,
+                    install=False)
+    assert abs(w @ (v2 - v0) - dsc @ ds) <= 1e-8 * abs(dsc @ ds) + 1e-12
+
+
+@pytest.mark.slow
+def test_in13_fixture_end_to_end():
+    """The reference's published In13_P16 run, reproduced on the GPU."""
+    from tests import fixture_in13
+
+    f = fixture_in13.load()
+    n = int(np.prod(f["dims"]))
+    ctx = sep.Context(f["dims"], f["steps"])
+    types = f["types"].astype(np.int32)
+    pot = ctx.vbuild(f["xyz"], types, f["tab_r"], f["tab_v_shifted"], f["tab_n"], f["mins"],
+                     scale=f["strain_scale"], install=True)
+    ref_pot = O.vbuild(*f["xyz"].T, f["types"], f["tab_r"], f["tab_v_shifted"], f["tab_n"],
+                       f["dims"], f["mins"], f["steps"], scale=f["strain_scale"])
+    assert np.array_equal(pot, ref_pot)
+    assert abs(pot.min() - f["vmin"]) < 1e-5 and abs(pot.max() - f["vmax"]) < 1e-5
+    start = sep.start_states(f["seed"], int(f["ns"]), n, f["dv"])
+    res = ctx.pipeline(start, f["el"], int(f["nc"]), float(pot.min()))
+    assert abs(res["timing"]["dE"] - f["dE"]) < 1e-4
+    ev, sg = res["eval"], res["sigma"]
+    ref_ev, ref_sg = f["eval"], f["sigma"]
+    win = (ref_ev > -0.25) & (ref_ev < 0.0) & (ref_sg < 1e-5)
+    for e in ref_ev[win]:
+        j = np.argmin(np.abs(ev - e))
+        assert abs(ev[j] - e) < 1e-6 and sg[j] < 1e-5, (e, ev[j], sg[j])
+    mine = (ev > -0.25) & (ev < 0.0) & (sg < 1e-5)
+    assert mine.sum() == win.sum()
+    # portho keeps S_i/S_0 >= 1e-10: 158 states in the fixture's run.dat
+    assert abs(res["mkept"] - int(f["cutoff"])) <= 2, res["mkept"]
