@@ -46,8 +46,9 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="skip FP64 sample, pipeline, roofline and CPU baseline")
     p.add_argument("--profile", choices=["mixed", "f64"], default=None,
-                   help="run only a small filter case for an ncu capture: 24 start states "
-                        "x 8 Newton steps of the 128^3 workload (about 3.5 GB on the device)")
+                   help="run only a small filter case for an ncu capture: 24 (mixed) or 16 "
+                        "(f64) start states x 8 Newton steps of the 128^3 workload (3.5 GB "
+                        "and 4.8 GB on the device)")
     return p.parse_args()
 
 
@@ -65,10 +66,11 @@ def run_profile(args):
     dE = 80.0
     nc = 9
     an_re, _, zn = sep.coefficients(S.el, nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
-    start = sep.start_states(START_SEED, 24, S.ngrid, S.dv)
+    nstates = 24 if args.profile == "mixed" else 16
+    start = sep.start_states(START_SEED, nstates, S.ngrid, S.dv)
     for _ in range(2):
         out = ctx.filter(start, an_re, zn, 4.0 / dE, vmin)
-    print(json.dumps({"profile_case": args.profile, "states": 24, "newton_steps": nc - 1,
+    print(json.dumps({"profile_case": args.profile, "states": nstates, "newton_steps": nc - 1,
                       "checksum": float(np.abs(out).sum())}))
 
 

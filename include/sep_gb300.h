@@ -76,6 +76,25 @@ int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
 int sep_hamiltonian(sep_ctx *ctx, const double *psi, double *hpsi, long nstates);
 int sep_hamiltonian_dev(sep_ctx *ctx, const double *psi, double *hpsi, long nstates);
 
+/* ---- general apply: out = alpha (T x + V y) + beta y ----------------------
+ * Covers kinetic (y = NULL: out = alpha T x, filter/hamiltonian.c:27-44),
+ * hamiltonian_norm (T phi + V psi, filter/hnorm.c:29-39) and hnorm. */
+int sep_apply(sep_ctx *ctx, const double *x, const double *y, double *out, long nstates,
+              double alpha, double beta);
+/* Override the kinetic cap with an already 1/N-scaled value (the reference's
+ * par.Ekinmax after filter/init.c:137). */
+int sep_ctx_set_kcap(sep_ctx *ctx, double kcap_scaled);
+/* out[r] = sum_g x[r][g]^2 for m rows of len doubles, without a context. */
+int sep_row_sumsq(const double *x, long m, long len, double *out);
+/* The context's k^2 grid (ngrid doubles) with its current cap. */
+int sep_ctx_ksqr(sep_ctx *ctx, double *out);
+/* filter/norm.c:40-54 without a context (any ngrid). */
+int sep_normalize_states(double *psi, long m, long ngrid, double dv);
+/* filter/rand.c:28-66 ran_nrc with its process-wide shuffle state, and
+ * filter/init.c:236-251 init_psi drawing from it (real parts; *idum advances). */
+double sep_ran_nrc(long *idum);
+int sep_init_psi(long *idum, long ngrid, double dv, double *psi_re);
+
 /* ---- filter/hnorm.c:11-39 ------------------------------------------------
  * psin = dE_1 H psim1 - (2 + zm1 + vmin dE_1) psim1 (complex grids). */
 int sep_hnorm(sep_ctx *ctx, const double *psim1, double *psin, long nstates, double dE_1,

@@ -68,9 +68,9 @@ template <typename T> int upload_grid(sep_ctx* c, GridDev<T>& g) {
   return kOk;
 }
 
-int check_ctx(sep_ctx* c) {
+int check_ctx(sep_ctx* c, bool need_pot = true) {
   if (!c) return arg_fail("null context");
-  if (!c->have_pot) return arg_fail("the context has no potential yet");
+  if (need_pot && !c->have_pot) return arg_fail("the context has no potential yet");
   CK(cudaSetDevice(c->device));
   return kOk;
 }
@@ -272,6 +272,90 @@ int sep_hamiltonian(sep_ctx* c, const double* psi, double* hpsi, long nstates) {
   return kOk;
 }
 
+int sep_apply(sep_ctx* c, const double* x, const double* y, double* out, long nstates,
+              double alpha, double beta) {
+  RET(check_ctx(c));
+  if (!x || !out || nstates < 1) return arg_fail("sep_apply: bad argument");
+  const size_t cnt = 2 * (size_t)c->n * nstates;
+  RET(to_device(c, c->w_start, x, cnt));
+  if (y) RET(to_device(c, c->w_states, y, cnt));
+  RET(ensure_buf(c, c->w_out, cnt * sizeof(double)));
+  RET(ensure_buf(c, c->w_fft, sizeof(cx<double>) * (size_t)c->n * nstates));
+  CK(apply_txvy<double>(c->g64, c->w_start.as<cx<double>>(),
+                        y ? c->w_states.as<cx<double>>() : nullptr, c->w_out.as<cx<double>>(),
+                        c->w_fft.as<cx<double>>(), (int)nstates, alpha, beta, c->stream));
+  CK(cudaMemcpyAsync(out, c->w_out.p, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return kOk;
+}
+
+int sep_ctx_set_kcap(sep_ctx* c, double kcap) {
+  if (!c || !(kcap > 0.0)) return arg_fail("sep_ctx_set_kcap: bad argument");
+  c->ktab.cap = kcap;
+  c->g64.kcap = kcap;
+  c->g32.kcap = (float)kcap;
+  for (auto& g : c->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return kOk;
+}
+
+int sep_normalize_states(double* psi, long m, long ngrid, double dv) {
+  if (!psi || m < 1 || ngrid < 1 || !(dv > 0.0)) return arg_fail("sep_normalize_states: bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    sep::set_error("sep_normalize_states: no CUDA device");
+    return kErrNoDevice;
+  }
+  const size_t cnt = (size_t)m * ngrid;
+  double *d = nullptr, *red = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * cnt));
+  cudaError_t e = cudaMalloc(&red, sizeof(double) * (reduce_partial_doubles(m) + m + 64));
+  if (e == cudaSuccess) e = cudaMemcpy(d, psi, sizeof(double) * cnt, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = normalize_rows<double>(d, m, ngrid, dv, red, red + reduce_partial_doubles(m), 0);
+  if (e == cudaSuccess) e = cudaMemcpy(psi, d, sizeof(double) * cnt, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (red) cudaFree(red);
+  if (e != cudaSuccess) return cuda_fail(e, "sep_normalize_states", __LINE__);
+  return kOk;
+}
+
+int sep_row_sumsq(const double* x, long m, long len, double* out) {
+  if (!x || !out || m < 1 || len < 1) return arg_fail("sep_row_sumsq: bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    sep::set_error("sep_row_sumsq: no CUDA device");
+    return kErrNoDevice;
+  }
+  const size_t cnt = (size_t)m * len;
+  double *d = nullptr, *red = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * cnt));
+  cudaError_t e = cudaMalloc(&red, sizeof(double) * (reduce_partial_doubles(m) + m + 64));
+  if (e == cudaSuccess) e = cudaMemcpy(d, x, sizeof(double) * cnt, cudaMemcpyHostToDevice);
+  double* res = red ? red + reduce_partial_doubles(m) : nullptr;
+  if (e == cudaSuccess) e = row_dots<double>(d, d, m, len, 1.0, res, red, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, res, sizeof(double) * m, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (red) cudaFree(red);
+  if (e != cudaSuccess) return cuda_fail(e, "sep_row_sumsq", __LINE__);
+  return kOk;
+}
+
+int sep_ctx_ksqr(sep_ctx* c, double* out) {
+  if (!c || !out) return arg_fail("sep_ctx_ksqr: null argument");
+  host::ksqr_grid(c->ktab, c->nx, c->ny, c->nz, out);
+  return kOk;
+}
+
+double sep_ran_nrc(long* idum) { return host::global_ran_nrc(idum); }
+
+int sep_init_psi(long* idum, long ngrid, double dv, double* psi_re) {
+  if (!idum || !psi_re || ngrid < 1) return arg_fail("sep_init_psi: bad argument");
+  host::global_init_psi(idum, ngrid, dv, psi_re);
+  return kOk;
+}
+
 int sep_hnorm(sep_ctx* c, const double* psim1, double* psin, long nstates, double dE_1,
               double vmin, double zm1) {
   RET(check_ctx(c));
@@ -314,7 +398,7 @@ int sep_filter(sep_ctx* c, const double* start, long ns, const double* an_re, co
 
 // ---- norms and energies --------------------------------------------------
 int sep_normalize_all(sep_ctx* c, double* psi, long m) {
-  RET(check_ctx(c));
+  RET(check_ctx(c, false));
   if (!psi || m < 1) return arg_fail("sep_normalize_all: bad argument");
   RET(to_device(c, c->w_start, psi, (size_t)c->n * m));
   RET(normalize_device(c, c->w_start.as<double>(), m));
@@ -339,7 +423,7 @@ int sep_energy_range(sep_ctx* c, double vmin, double* emax, double* dE, long* it
 
 // ---- subspace ------------------------------------------------------------
 int sep_ortho(sep_ctx* c, double* psi, long m, long* mkept) {
-  RET(check_ctx(c));
+  RET(check_ctx(c, false));
   if (!psi || !mkept || m < 1) return arg_fail("sep_ortho: bad argument");
   RET(to_device(c, c->w_start, psi, (size_t)c->n * m));
   RET(ortho_device(c, c->w_start.as<double>(), m, mkept));

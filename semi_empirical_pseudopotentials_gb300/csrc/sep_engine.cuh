@@ -46,6 +46,12 @@ template <typename T>
 cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& io, int B,
                      cudaStream_t s);
 
+// out = alpha (T x + V y) + beta y for B complex grids; y may be null (out = alpha T x).
+// scratch: B * n complex; out may not alias x.
+template <typename T>
+cudaError_t apply_txvy(const GridDev<T>& g, const cx<T>* x, const cx<T>* y, cx<T>* out,
+                       cx<T>* scratch, int B, T alpha, T beta, cudaStream_t s);
+
 // H (or alpha H + beta) applied to B complex grids: out = alpha (T in + V in) + beta in.
 // scratch: B * n complex.  out may not alias in.
 template <typename T>

@@ -35,7 +35,7 @@ enum PassMode : int {
 template <typename T> struct PassArgs {
   cx<T>* data;            // transformed in place
   const cx<T>* src;       // kFwd: read from here instead of data when not null
-  const cx<T>* psi_in;    // epilogue: previous state
+  const cx<T>* psi_in;    // epilogue: previous state (null: no V and no beta term)
   cx<T>* psi_out;         // epilogue: new state
   const T* pot;           // epilogue: V on the grid (shared by the batch)
   const cx<T>* tw;        // exp(-2 pi i m / L), m < L, for this axis
@@ -83,7 +83,7 @@ template <typename T, int L, int AXIS> struct Tile {
   // x: about 128 threads per block
   static constexpr int tl_raw = (AXIS == 0) ? ((128 / nmin) > 0 ? 128 / nmin : 1) : 16;
   // keep the exchange buffer under 40 KB of static shared memory
-  static constexpr int bytes_per_line = L * (int)sizeof(cx<T>) + 16 * (int)sizeof(cx<T>);
+  static constexpr int bytes_per_line = L * (int)sizeof(cx<T>) + 32 * (int)sizeof(cx<T>);
   static constexpr int tl_cap = (40 * 1024) / bytes_per_line;
   static constexpr int tl = tl_raw < tl_cap ? tl_raw : (tl_cap >= 8 ? 8 : tl_cap);
   static constexpr int nt = tl * nmin;
@@ -100,8 +100,12 @@ line_pass(PassArgs<T> a) {
   constexpr int IA = (NA + NT - 1) / NT, IB = (NB + NT - 1) / NT;
   constexpr int PAD = (AXIS == 0) ? 1 : 0;
   constexpr int SROW = N1 + PAD;  // x axis: [line][b][a + pad]
+  // x axis: lines start 8 elements off a multiple of 16 so that the lines a
+  // warp touches at once fall on different banks
+  constexpr int LSTR =
+      (AXIS == 0) ? N2 * SROW + ((8 - (N2 * SROW) % 16) + 16) % 16 : N2 * SROW;
 
-  __shared__ C sh[TL * N2 * SROW];
+  __shared__ C sh[(AXIS == 0) ? TL * LSTR : TL * N2 * SROW];
   __shared__ C tws[L];
 
   const int tid = threadIdx.x;
@@ -109,7 +113,7 @@ line_pass(PassArgs<T> a) {
 
   // shared index of element (line, a in [0,N1), b in [0,N2))
   auto sidx = [&](int line, int ia, int ib) -> int {
-    if constexpr (AXIS == 0) return (line * N2 + ib) * SROW + ia;
+    if constexpr (AXIS == 0) return line * LSTR + ib * SROW + ia;
     else return (ia * N2 + ib) * TL + line;
   };
 
@@ -318,13 +322,13 @@ line_pass(PassArgs<T> a) {
       if ((NA % NT == 0 || i < NA) && line < nvalid) {
         const long long lb = base0 + line * lstride;          // offset in the batch array
         const long long gb = lb % N;                          // offset in one grid
-        const C* pin = a.psi_in + lb;
+        const C* pin = a.psi_in ? a.psi_in + lb : nullptr;
         C* pout = a.psi_out + lb;
         const T* pv = a.pot + gb;
 #pragma unroll
         for (int n2 = 0; n2 < N2; ++n2) {
           const int x = n1 + N1 * n2;
-          const C p = pin[x];
+          const C p = pin ? pin[x] : mk<T>(T(0), T(0));
           const T v = pv[x];
           C h = mk<T>(va[r][n2].x + v * p.x, va[r][n2].y + v * p.y);
           C o = mk<T>(alpha * h.x + beta * p.x, alpha * h.y + beta * p.y);

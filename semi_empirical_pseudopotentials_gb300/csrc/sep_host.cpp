@@ -118,6 +118,29 @@ double Rand::next() {
   return t > top ? top : t;
 }
 
+namespace {
+Rand& global_rand() {
+  static Rand r(0);
+  return r;
+}
+}  // namespace
+
+double global_ran_nrc(long* idum) {
+  Rand& r = global_rand();
+  r.idum = *idum;
+  const double v = r.next();
+  *idum = r.idum;
+  return v;
+}
+
+void global_init_psi(long* idum, long ngrid, double dv, double* out) {
+  // init_psi copies *idum into a local, draws, and writes it back (init.c:239-249)
+  Rand& r = global_rand();
+  r.idum = *idum;
+  init_psi(r, ngrid, dv, out);
+  *idum = r.idum;
+}
+
 void init_psi(Rand& r, long ngrid, double dv, double* out) {
   for (long g = 0; g < ngrid; ++g) out[g] = -1.0 + 2.0 * r.next();
   double s = 0.0;

@@ -24,6 +24,12 @@ struct Rand {
 // filter/init.c:236-251 (normalize of norm.c:9-36 divides by the norm)
 void init_psi(Rand& r, long ngrid, double dv, double* out);
 
+// The reference's ran_nrc keeps its second stream and shuffle table in
+// statics shared by the whole process (filter/rand.c:32-34); these two entry
+// points reproduce that, with *idum as the caller's running seed.
+double global_ran_nrc(long* idum);
+void global_init_psi(long* idum, long ngrid, double dv, double* out);
+
 // filter/init.c:124-144: per-axis tables and the cap
 struct KTables {
   std::vector<double> kx, ky, kz;

@@ -50,22 +50,29 @@ __global__ void __launch_bounds__(kThreads)
 k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long long j0,
              int count, const TA* __restrict__ an, long long nc, int ms, TA* __restrict__ acc,
              long long nstates, int init) {
+  // grid.y = pair b; grid-stride over the grid points of that pair; the slot
+  // offsets and coefficients are resolved once per block
   __shared__ TA cf[MSMAX * kMaxBlockSteps];
+  __shared__ long long soff[kMaxBlockSteps];
   for (int i = threadIdx.x; i < ms * count; i += blockDim.x) {
     const int e = i / count, s = i - e * count;
     cf[e * kMaxBlockSteps + s] = an[e * nc + j0 + s];
   }
+  const long long b = blockIdx.y;
+  for (int s = threadIdx.x; s < count; s += blockDim.x)
+    soff[s] = (long long)((j0 + s) % slots) * ((long long)B * n) + b * n;
   __syncthreads();
-  const long long total = (long long)B * n;
-  const long long slot_stride = total;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long b = i / n, g = i - b * n;
+  const long long s0 = 2 * b, s1 = 2 * b + 1;
+  const bool two = s1 < nstates;
+  TA* __restrict__ a0 = acc + s0 * ms * n;
+  TA* __restrict__ a1 = acc + s1 * ms * n;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+       g += (long long)gridDim.x * blockDim.x) {
     TA re[MSMAX], im[MSMAX];
 #pragma unroll
     for (int e = 0; e < MSMAX; ++e) { re[e] = TA(0); im[e] = TA(0); }
     for (int s = 0; s < count; ++s) {
-      const cx<T> h = hist[((j0 + s) % slots) * slot_stride + i];
+      const cx<T> h = hist[soff[s] + g];
 #pragma unroll
       for (int e = 0; e < MSMAX; ++e) {
         if (e < ms) {
@@ -75,14 +82,13 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
         }
       }
     }
-    const long long s0 = 2 * b, s1 = 2 * b + 1;
 #pragma unroll
     for (int e = 0; e < MSMAX; ++e) {
       if (e < ms) {
-        TA* p0 = acc + (s0 * ms + e) * n + g;
+        TA* p0 = a0 + e * n + g;
         *p0 = init ? re[e] : *p0 + re[e];
-        if (s1 < nstates) {
-          TA* p1 = acc + (s1 * ms + e) * n + g;
+        if (two) {
+          TA* p1 = a1 + e * n + g;
           *p1 = init ? im[e] : *p1 + im[e];
         }
       }
@@ -404,8 +410,14 @@ template <typename T, typename TA>
 cudaError_t newton_accumulate(const cx<T>* hist, int slots, int B, long long n, long long j0,
                               int count, const TA* an, long long nc, int ms, TA* acc,
                               long long nstates, bool init, cudaStream_t s) {
-  if (count < 1 || count > kMaxBlockSteps || ms < 1 || ms > 32) return cudaErrorInvalidValue;
-  const unsigned g = blocks_for((long long)B * n, kThreads, 152LL * 16);
+  if (count < 1 || count > kMaxBlockSteps || ms < 1 || ms > 32 || B > 65535)
+    return cudaErrorInvalidValue;
+  // about 4 blocks of 256 threads per SM in total, spread over the pairs
+  long long per = (152LL * 4 + B - 1) / B;
+  const long long need = (n + kThreads - 1) / kThreads;
+  if (per > need) per = need;
+  if (per < 1) per = 1;
+  const dim3 g((unsigned)per, (unsigned)B);
   if (ms <= 4)
     k_accumulate<T, TA, 4><<<g, kThreads, 0, s>>>(hist, slots, B, n, j0, count, an, nc, ms, acc,
                                                   nstates, init);

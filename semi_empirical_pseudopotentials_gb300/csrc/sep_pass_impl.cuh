@@ -78,6 +78,26 @@ cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
 }
 
 template <>
+cudaError_t apply_txvy<SEP_T>(const GridDev<SEP_T>& g, const cx<SEP_T>* x, const cx<SEP_T>* y,
+                              cx<SEP_T>* out, cx<SEP_T>* scratch, int B, SEP_T alpha,
+                              SEP_T beta, cudaStream_t s) {
+  cudaError_t e;
+  PassIO<SEP_T> io;
+  io.data = scratch;
+  io.src = x;
+  if ((e = run_pass<SEP_T>(0, kFwd, g, io, B, s))) return e;
+  io.src = nullptr;
+  if ((e = run_pass<SEP_T>(1, kFwd, g, io, B, s))) return e;
+  if ((e = run_pass<SEP_T>(2, kFwdKInv, g, io, B, s))) return e;
+  if ((e = run_pass<SEP_T>(1, kInv, g, io, B, s))) return e;
+  io.psi_in = y;
+  io.psi_out = out;
+  io.alpha = alpha;
+  io.beta = beta;
+  return run_pass<SEP_T>(0, kInvEpi, g, io, B, s);
+}
+
+template <>
 cudaError_t apply_h<SEP_T>(const GridDev<SEP_T>& g, const cx<SEP_T>* in, cx<SEP_T>* out,
                            cx<SEP_T>* scratch, int B, SEP_T alpha, SEP_T beta,
                            cudaStream_t s) {
