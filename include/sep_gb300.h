@@ -68,7 +68,7 @@ int sep_ctx_info(sep_ctx *ctx, double *vmin, double *vmax, double *dv, long *ngr
 int sep_ctx_stream(sep_ctx *ctx, void **cuda_stream);             /* cudaStream_t */
 /* Capture the Newton loop of sep_filter* in a CUDA graph (default 1). */
 int sep_ctx_set_graphs(sep_ctx *ctx, int enable);
-/* Newton steps accumulated per pass over the step history (default 16). */
+/* Newton steps accumulated per pass over the step history (default 32). */
 int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
 
 /* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------
@@ -170,6 +170,12 @@ int sep_vbuild_backward(sep_ctx *ctx, long natom, const double *xyz, const int *
                         const double *tab_v, const long *tab_n, long tab_stride,
                         const double mins[3], const double *dpotl, double *dtab_v,
                         double *dscale);
+
+/* Hellmann-Feynman: rho[g] = dv sum_k w[k] psi[k][g]^2 for m real states
+ * (host arrays).  For normalised eigenstates, dE_k/dV(r_g) = psi_k(r_g)^2 dv,
+ * so with w = dL/dE this is dL/dpotl for sep_vbuild_backward.  No
+ * counterpart in the reference (it has no gradients). */
+int sep_hf_density(sep_ctx *ctx, const double *psi, long m, const double *w, double *rho);
 
 /* ---- measurement --------------------------------------------------------
  * Average device time (ms, CUDA events on the context stream) of one launch

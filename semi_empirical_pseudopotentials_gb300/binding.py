@@ -80,6 +80,7 @@ def lib():
         L.sep_vbuild_backward.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, dp, lp,
                                           C.c_long, dp, dp, dp, dp]
         L.sep_time_passes.argtypes = [vp, C.c_long, C.c_int, dp]
+        L.sep_hf_density.argtypes = [vp, dp, C.c_long, dp, dp]
         _lib = L
     return _lib
 
@@ -281,6 +282,14 @@ class Context:
         return {"eval": ev[:kk], "sigma": sg[:kk], "mkept": kk,
                 "psi": None if psi is None else psi[:kk],
                 "timing": {f: getattr(t, f) for f, _ in Timing._fields_}}
+
+    def hf_density(self, psi, w):
+        """rho = dv sum_k w_k psi_k^2 (Hellmann-Feynman dL/dV for normalised states)."""
+        psi = _f64(psi).reshape(-1, self.ngrid)
+        w = _f64(w)
+        rho = np.empty(self.ngrid)
+        _check(lib().sep_hf_density(self.h, _p(psi), psi.shape[0], _p(w), _p(rho)))
+        return rho
 
     def time_passes(self, npairs, reps=10):
         """Average ms per launch: x fwd, y fwd, z fwd*k*inv, y inv, x inv+epi+fwd, accumulate."""

@@ -342,6 +342,20 @@ int sep_row_sumsq(const double* x, long m, long len, double* out) {
   return kOk;
 }
 
+int sep_hf_density(sep_ctx* c, const double* psi, long m, const double* w, double* rho) {
+  RET(check_ctx(c, false));
+  if (!psi || !w || !rho || m < 1) return arg_fail("sep_hf_density: bad argument");
+  RET(to_device(c, c->w_start, psi, (size_t)c->n * m));
+  RET(to_device(c, c->w_coef, w, (size_t)m));
+  RET(ensure_buf(c, c->w_out, sizeof(double) * (size_t)c->n));
+  CK(weighted_density(c->w_start.as<double>(), c->w_coef.as<double>(), m, c->n, c->dv,
+                      c->w_out.as<double>(), c->stream));
+  CK(cudaMemcpyAsync(rho, c->w_out.p, sizeof(double) * c->n, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return kOk;
+}
+
 int sep_ctx_ksqr(sep_ctx* c, double* out) {
   if (!c || !out) return arg_fail("sep_ctx_ksqr: null argument");
   host::ksqr_grid(c->ktab, c->nx, c->ny, c->nz, out);

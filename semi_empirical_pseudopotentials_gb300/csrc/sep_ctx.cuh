@@ -48,7 +48,7 @@ struct sep_ctx {
   double vmin = 0, vmax = 0;
   bool have_pot = false;
   bool use_graphs = true;
-  int block_steps = 16;
+  int block_steps = 32;
   sep::host::KTables ktab;
   sep::GridDev<double> g64;
   sep::GridDev<float> g32;

@@ -25,7 +25,16 @@ template <typename T> struct GridDev {
   T* kz = nullptr;
   T kcap = 0;
   T* pot = nullptr;
+  int variant[5] = {0, 0, 0, 0, 0};  // tile shape per pass kind (autotuned)
 };
+
+// pass kinds of a Newton step: x forward, y forward, z forward*k^2*inverse,
+// y inverse, x inverse + epilogue (+ forward)
+inline int pass_kind(int axis, int mode) {
+  if (axis == 0) return mode == kFwd ? 0 : 4;
+  if (axis == 1) return mode == kFwd ? 1 : 3;
+  return 2;
+}
 
 // lengths with a compiled line pass
 bool length_supported(int L);
@@ -39,6 +48,7 @@ template <typename T> struct PassIO {
   T alpha = T(1), beta = T(0);
   const T* coefs = nullptr;  // device (alpha, beta) per step
   int step = 0;
+  int variant = -1;          // -1: the grid's autotuned choice
 };
 
 // One line pass over a batch of B grids (see sep_fftpass.cuh for modes).

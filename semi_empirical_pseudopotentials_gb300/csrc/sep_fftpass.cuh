@@ -75,27 +75,34 @@ SEP_SPLIT(192, 12, 16)
 SEP_SPLIT(256, 16, 16)
 #undef SEP_SPLIT
 
-// lines handled by one block: x axis -> whole lines, y/z -> adjacent x
-template <typename T, int L, int AXIS> struct Tile {
+// lines handled by one block: x axis -> whole lines, y/z -> adjacent x.
+// Two shapes per pass (V = 0, 1); the autotuner picks one per context.
+template <typename T, int L, int AXIS, int V = 0> struct Tile {
   static constexpr int n1 = Split<L>::n1, n2 = Split<L>::n2;
   static constexpr int nmin = n1 < n2 ? n1 : n2;
-  // y/z: 16 adjacent x (256 B of complex128, 128 B of complex64 per row);
-  // x: about 128 threads per block
-  static constexpr int tl_raw = (AXIS == 0) ? ((128 / nmin) > 0 ? 128 / nmin : 1) : 16;
+  // V0 -- y/z: 16 adjacent x (256 B of complex128, 128 B of complex64 per
+  // row); x: about 128 threads per block.
+  // V1 -- y/z: 8 adjacent x for complex128, 32 for complex64; x: about 256
+  // threads per block.
+  static constexpr int yz_lines = (V == 0) ? 16 : (sizeof(T) == 8 ? 8 : 32);
+  static constexpr int x_threads = (V == 0) ? 128 : 256;
+  static constexpr int tl_raw =
+      (AXIS == 0) ? ((x_threads / nmin) > 0 ? x_threads / nmin : 1) : yz_lines;
   // keep the exchange buffer under 40 KB of static shared memory
   static constexpr int bytes_per_line = L * (int)sizeof(cx<T>) + 32 * (int)sizeof(cx<T>);
   static constexpr int tl_cap = (40 * 1024) / bytes_per_line;
-  static constexpr int tl = tl_raw < tl_cap ? tl_raw : (tl_cap >= 8 ? 8 : tl_cap);
+  static constexpr int pow2_floor(int v) { return v >= 2 ? 2 * pow2_floor(v / 2) : 1; }
+  static constexpr int tl = pow2_floor(tl_raw < tl_cap ? tl_raw : (tl_cap > 0 ? tl_cap : 1));
   static constexpr int nt = tl * nmin;
 };
 
-template <typename T, int L, int AXIS, int MODE>
-__global__ void __launch_bounds__(Tile<T, L, AXIS>::nt)
+template <typename T, int L, int AXIS, int MODE, int V = 0>
+__global__ void __launch_bounds__(Tile<T, L, AXIS, V>::nt)
 line_pass(PassArgs<T> a) {
   using C = cx<T>;
   constexpr int N1 = Split<L>::n1, N2 = Split<L>::n2;
-  constexpr int TL = Tile<T, L, AXIS>::tl;
-  constexpr int NT = Tile<T, L, AXIS>::nt;
+  constexpr int TL = Tile<T, L, AXIS, V>::tl;
+  constexpr int NT = Tile<T, L, AXIS, V>::nt;
   constexpr int NA = TL * N1, NB = TL * N2;
   constexpr int IA = (NA + NT - 1) / NT, IB = (NB + NT - 1) / NT;
   constexpr int PAD = (AXIS == 0) ? 1 : 0;

@@ -43,7 +43,7 @@ __global__ void k_unpack(const cx<T>* __restrict__ in, long long nstates, long l
 }
 
 // -------------------------------------------------------------------------
-constexpr int kMaxBlockSteps = 64;
+constexpr int kMaxBlockSteps = 64;  // history grids per accumulation pass
 
 template <typename T, typename TA, int MSMAX>
 __global__ void __launch_bounds__(kThreads)
@@ -412,10 +412,10 @@ cudaError_t newton_accumulate(const cx<T>* hist, int slots, int B, long long n, 
                               long long nstates, bool init, cudaStream_t s) {
   if (count < 1 || count > kMaxBlockSteps || ms < 1 || ms > 32 || B > 65535)
     return cudaErrorInvalidValue;
-  // about 4 blocks of 256 threads per SM in total, spread over the pairs
-  long long per = (152LL * 4 + B - 1) / B;
-  const long long need = (n + kThreads - 1) / kThreads;
-  if (per > need) per = need;
+  // each thread sees about 4 grid points of one pair (enough blocks to keep
+  // 64 warps per SM resident while the history loads are in flight)
+  long long per = (n + 4LL * kThreads - 1) / (4LL * kThreads);
+  if (per > 65535) per = 65535;
   if (per < 1) per = 1;
   const dim3 g((unsigned)per, (unsigned)B);
   if (ms <= 4)
@@ -568,6 +568,28 @@ __global__ void k_sub_2d(double* __restrict__ dst, long long ld, const double* _
 cudaError_t sub_2d_f64(double* dst, long long ld, const double* src, long long rows,
                        long long w, cudaStream_t s) {
   k_sub_2d<<<blocks_for(rows * w, kThreads), kThreads, 0, s>>>(dst, ld, src, rows, w);
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void k_weighted_density(const double* __restrict__ psi, const double* __restrict__ w,
+                                   long long m, long long n, double dv,
+                                   double* __restrict__ rho) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+       g += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (long long k = 0; k < m; ++k) {
+      const double p = psi[k * n + g];
+      s += w[k] * p * p;
+    }
+    rho[g] = s * dv;
+  }
+}
+}  // namespace
+
+cudaError_t weighted_density(const double* psi, const double* w, long long m, long long n,
+                             double dv, double* rho, cudaStream_t s) {
+  k_weighted_density<<<blocks_for(n, kThreads), kThreads, 0, s>>>(psi, w, m, n, dv, rho);
   return cudaGetLastError();
 }
 

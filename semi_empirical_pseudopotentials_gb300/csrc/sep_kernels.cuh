@@ -56,6 +56,9 @@ cudaError_t gemm_nn_f64_ld(const double* A, const double* B, long long M, long l
 // dst[r][c] -= src[r][c] for r < rows, c < w (dst rows ld apart, src dense)
 cudaError_t sub_2d_f64(double* dst, long long ld, const double* src, long long rows,
                        long long w, cudaStream_t s);
+// rho[g] = dv * sum_k w[k] psi[k][g]^2 (Hellmann-Feynman weights)
+cudaError_t weighted_density(const double* psi, const double* w, long long m, long long n,
+                             double dv, double* rho, cudaStream_t s);
 // A <- (A + A^T) / 2, m x m
 cudaError_t symmetrize_f64(double* A, long long m, cudaStream_t s);
 // S[l][i] = R[l][i] / sqrt(lam[l]), k x k

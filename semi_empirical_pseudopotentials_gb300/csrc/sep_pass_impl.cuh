@@ -6,12 +6,10 @@
 
 namespace sep {
 
-namespace {
-
-template <typename T, int L, int AXIS, int MODE>
+template <typename T, int L, int AXIS, int MODE, int V>
 cudaError_t launch_one(const PassArgs<T>& a, int B, cudaStream_t s) {
-  constexpr int TL = Tile<T, L, AXIS>::tl;
-  constexpr int NT = Tile<T, L, AXIS>::nt;
+  constexpr int TL = Tile<T, L, AXIS, V>::tl;
+  constexpr int NT = Tile<T, L, AXIS, V>::nt;
   dim3 grid;
   if (AXIS == 0) {
     long long blocks = (a.nbatch_lines + TL - 1) / TL;
@@ -22,27 +20,48 @@ cudaError_t launch_one(const PassArgs<T>& a, int B, cudaStream_t s) {
     if (other > 65535 || B > 65535) return cudaErrorInvalidValue;
     grid = dim3((unsigned)((a.nx + TL - 1) / TL), (unsigned)other, (unsigned)B);
   }
-  line_pass<T, L, AXIS, MODE><<<grid, NT, 0, s>>>(a);
+  line_pass<T, L, AXIS, MODE, V><<<grid, NT, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-template <typename T, int L>
+template <typename T, int L, int V>
 cudaError_t launch_len(int axis, int mode, const PassArgs<T>& a, int B, cudaStream_t s) {
   if (axis == 0) {
-    if (mode == kFwd) return launch_one<T, L, 0, kFwd>(a, B, s);
-    if (mode == kInvEpi) return launch_one<T, L, 0, kInvEpi>(a, B, s);
-    if (mode == kInvEpiFwd) return launch_one<T, L, 0, kInvEpiFwd>(a, B, s);
+    if (mode == kFwd) return launch_one<T, L, 0, kFwd, V>(a, B, s);
+    if (mode == kInvEpi) return launch_one<T, L, 0, kInvEpi, V>(a, B, s);
+    if (mode == kInvEpiFwd) return launch_one<T, L, 0, kInvEpiFwd, V>(a, B, s);
   } else if (axis == 1) {
-    if (mode == kFwd) return launch_one<T, L, 1, kFwd>(a, B, s);
-    if (mode == kInv) return launch_one<T, L, 1, kInv>(a, B, s);
+    if (mode == kFwd) return launch_one<T, L, 1, kFwd, V>(a, B, s);
+    if (mode == kInv) return launch_one<T, L, 1, kInv, V>(a, B, s);
   } else if (axis == 2) {
-    if (mode == kFwdKInv) return launch_one<T, L, 2, kFwdKInv>(a, B, s);
+    if (mode == kFwdKInv) return launch_one<T, L, 2, kFwdKInv, V>(a, B, s);
   }
   return cudaErrorInvalidValue;
 }
 
-}  // namespace
+// launch of one tile variant; each (precision, variant) lives in its own
+// translation unit so they compile in parallel
+template <typename T, int V>
+cudaError_t launch_variant(int axis, int mode, int L, const PassArgs<T>& a, int B,
+                           cudaStream_t s);
 
+#ifdef SEP_V
+template <>
+cudaError_t launch_variant<SEP_T, SEP_V>(int axis, int mode, int L, const PassArgs<SEP_T>& a,
+                                         int B, cudaStream_t s) {
+  switch (L) {
+#define SEP_CASE(LL) \
+  case LL: return launch_len<SEP_T, LL, SEP_V>(axis, mode, a, B, s);
+    SEP_CASE(16) SEP_CASE(18) SEP_CASE(20) SEP_CASE(24) SEP_CASE(32) SEP_CASE(36)
+    SEP_CASE(40) SEP_CASE(48) SEP_CASE(56) SEP_CASE(64) SEP_CASE(72) SEP_CASE(80)
+    SEP_CASE(96) SEP_CASE(112) SEP_CASE(128) SEP_CASE(160) SEP_CASE(192) SEP_CASE(256)
+#undef SEP_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+#endif
+
+#ifdef SEP_DISPATCH
 template <>
 cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
                             const PassIO<SEP_T>& io, int B, cudaStream_t s) {
@@ -66,15 +85,9 @@ cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
   a.ny = g.ny;
   a.nz = g.nz;
   const int L = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
-  switch (L) {
-#define SEP_CASE(LL) \
-  case LL: return launch_len<SEP_T, LL>(axis, mode, a, B, s);
-    SEP_CASE(16) SEP_CASE(18) SEP_CASE(20) SEP_CASE(24) SEP_CASE(32) SEP_CASE(36)
-    SEP_CASE(40) SEP_CASE(48) SEP_CASE(56) SEP_CASE(64) SEP_CASE(72) SEP_CASE(80)
-    SEP_CASE(96) SEP_CASE(112) SEP_CASE(128) SEP_CASE(160) SEP_CASE(192) SEP_CASE(256)
-#undef SEP_CASE
-    default: return cudaErrorInvalidValue;
-  }
+  const int v = io.variant >= 0 ? io.variant : g.variant[pass_kind(axis, mode)];
+  if (v == 1) return launch_variant<SEP_T, 1>(axis, mode, L, a, B, s);
+  return launch_variant<SEP_T, 0>(axis, mode, L, a, B, s);
 }
 
 template <>
@@ -116,5 +129,7 @@ cudaError_t apply_h<SEP_T>(const GridDev<SEP_T>& g, const cx<SEP_T>* in, cx<SEP_
   io.beta = beta;
   return run_pass<SEP_T>(0, kInvEpi, g, io, B, s);
 }
+
+#endif  // SEP_DISPATCH
 
 }  // namespace sep

@@ -89,3 +89,42 @@ def test_bad_arguments_raise():
         sep.coefficients([0.1], 0, 1.0, 0.0, 1.0)
     with pytest.raises(sep.SepError):
         sep.start_states(-1, 0, 10, 1.0)
+
+
+def test_form_factor_jacobian_matches_central_differences():
+    from semi_empirical_pseudopotentials_gb300 import adjoint
+
+    a = np.array([10.2, 1.45, 29.0, 0.31])
+    vol = 189.6
+    r, v, jac = adjoint.form_factor_jacobian(a, vol)
+    for j in range(4):
+        h = 1e-6 * max(1.0, abs(a[j]))
+        ap, am = a.copy(), a.copy()
+        ap[j] += h
+        am[j] -= h
+        fd = (sep.form_factor_table(ap, vol)[1] - sep.form_factor_table(am, vol)[1]) / (2 * h)
+        assert np.abs(fd - jac[j]).max() <= 1e-6 * np.abs(jac[j]).max() + 1e-12
+
+
+def test_shift_backward_is_the_adjoint():
+    from semi_empirical_pseudopotentials_gb300 import adjoint
+
+    rng = np.random.default_rng(0)
+    raw, d = rng.standard_normal(50), rng.standard_normal(50)
+    w = rng.standard_normal(50)
+
+    def shifted(x):
+        return x - x[-1]
+
+    lin = w @ (shifted(raw + 1e-3 * d) - shifted(raw)) / 1e-3
+    assert abs(lin - adjoint.shift_backward(w, 50) @ d) < 1e-9
+
+
+def test_band_edge_selection():
+    from semi_empirical_pseudopotentials_gb300 import adjoint
+
+    ev = np.array([-0.5, -0.45, -0.44, -0.43, -0.42, -0.2, -0.19, -0.18, -0.17, -0.1, 0.3])
+    sg = np.full_like(ev, 1e-8)
+    sg[-1] = 1.0
+    idx = adjoint.select_band_edges(ev, sg, 4)
+    assert list(ev[idx]) == [-0.45, -0.44, -0.43, -0.42, -0.2, -0.19, -0.18, -0.17]
