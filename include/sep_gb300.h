@@ -177,6 +177,34 @@ int sep_vbuild_backward(sep_ctx *ctx, long natom, const double *xyz, const int *
  * counterpart in the reference (it has no gradients). */
 int sep_hf_density(sep_ctx *ctx, const double *psi, long m, const double *w, double *rho);
 
+/* ---- many nanocrystals in one launch ---------------------------------------
+ * A batch holds one job per context (grids may differ): job j filters ns[j]
+ * start states with ms targets and nc Newton steps.  sep_batch_create
+ * captures every job's whole Newton filter as a parallel branch of ONE CUDA
+ * graph; sep_batch_run launches it once.  sep_batch_io returns each job's
+ * device start (ns x N) and output (ns x ms x N, float64) arrays; the
+ * coefficients of each job are uploaded before a run.  Each job needs its own
+ * context; while the batch exists, a context's filter workspace cannot grow
+ * (filters that fit it still run).  No counterpart in the reference (one
+ * program run per crystal). */
+typedef struct sep_batch sep_batch;
+int sep_batch_create(int njobs, sep_ctx *const *ctxs, const long *ns, long ms, long nc,
+                     sep_batch **out);
+int sep_batch_io(sep_batch *b, int job, double **start_dev, double **out_dev);
+int sep_batch_set_coefficients(sep_batch *b, int job, const double *an_re, const double *zn,
+                               double dE_1, double vmin);
+int sep_batch_run(sep_batch *b);
+/* host copies into / out of a job's device arrays */
+int sep_batch_load_start(sep_batch *b, int job, const double *host);
+int sep_batch_read_out(sep_batch *b, int job, double *host);
+int sep_batch_destroy(sep_batch *b);
+/* Tile-shape autotuner: times both compiled tile shapes of each of the 5
+ * Newton-step passes on npairs grids and keeps the faster per pass for this
+ * context; choices (5 ints, may be NULL) receives the picks. */
+int sep_ctx_autotune(sep_ctx *ctx, long npairs, int reps, int *choices);
+/* Set the 5 tile shapes (0 or 1) by hand. */
+int sep_ctx_set_tiles(sep_ctx *ctx, const int *choices);
+
 /* ---- measurement --------------------------------------------------------
  * Average device time (ms, CUDA events on the context stream) of one launch
  * of each Newton-step kernel on npairs complex grids in the context's

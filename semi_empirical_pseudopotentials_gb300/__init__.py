@@ -7,6 +7,7 @@ Nothing here computes on the CPU in place of the library: if the library is
 missing, every call raises.
 """
 from .binding import (  # noqa: F401
+    Batch,
     Context,
     SepError,
     coefficients,
@@ -17,5 +18,5 @@ from .binding import (  # noqa: F401
     start_states,
 )
 
-__all__ = ["Context", "SepError", "coefficients", "device_count", "form_factor_table", "ksqr",
+__all__ = ["Batch", "Context", "SepError", "coefficients", "device_count", "form_factor_table", "ksqr",
            "lib", "start_states"]

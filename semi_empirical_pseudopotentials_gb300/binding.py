@@ -81,6 +81,16 @@ def lib():
                                           C.c_long, dp, dp, dp, dp]
         L.sep_time_passes.argtypes = [vp, C.c_long, C.c_int, dp]
         L.sep_hf_density.argtypes = [vp, dp, C.c_long, dp, dp]
+        L.sep_ctx_autotune.argtypes = [vp, C.c_long, C.c_int, ip]
+        L.sep_batch_create.argtypes = [C.c_int, C.POINTER(vp), lp, C.c_long, C.c_long,
+                                       C.POINTER(vp)]
+        L.sep_batch_io.argtypes = [vp, C.c_int, C.POINTER(vp), C.POINTER(vp)]
+        L.sep_batch_set_coefficients.argtypes = [vp, C.c_int, dp, dp, C.c_double, C.c_double]
+        L.sep_batch_run.argtypes = [vp]
+        L.sep_batch_destroy.argtypes = [vp]
+        L.sep_batch_load_start.argtypes = [vp, C.c_int, dp]
+        L.sep_batch_read_out.argtypes = [vp, C.c_int, dp]
+        L.sep_ctx_set_tiles.argtypes = [vp, ip]
         _lib = L
     return _lib
 
@@ -291,6 +301,16 @@ class Context:
         _check(lib().sep_hf_density(self.h, _p(psi), psi.shape[0], _p(w), _p(rho)))
         return rho
 
+    def autotune(self, npairs, reps=5):
+        """Pick the faster tile shape per Newton-step pass; returns the 5 picks."""
+        ch = (C.c_int * 5)()
+        _check(lib().sep_ctx_autotune(self.h, npairs, reps, ch))
+        return list(ch)
+
+    def set_tiles(self, choices):
+        ch = (C.c_int * 5)(*[int(x) for x in choices])
+        _check(lib().sep_ctx_set_tiles(self.h, ch))
+
     def time_passes(self, npairs, reps=10):
         """Average ms per launch: x fwd, y fwd, z fwd*k*inv, y inv, x inv+epi+fwd, accumulate."""
         out = np.zeros(6)
@@ -328,3 +348,49 @@ class Context:
                                          tab_r.shape[1], _p(mins), _p(g), _p(dtab),
                                          None if dsc is None else _p(dsc)))
         return dtab, dsc
+
+
+class Batch:
+    """Several nanocrystals (one Context each, grids may differ) filtered by a
+    single CUDA graph launch (sep_batch_*)."""
+
+    def __init__(self, contexts, ns, ms, nc):
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        nsa = (C.c_long * len(self.contexts))(*[int(x) for x in ns])
+        h = C.c_void_p()
+        _check(lib().sep_batch_create(len(self.contexts), arr, nsa, ms, nc, C.byref(h)))
+        self.h = h
+        self.ns = [int(x) for x in ns]
+        self.ms, self.nc = ms, nc
+
+    def io(self, job):
+        s, o = C.c_void_p(), C.c_void_p()
+        _check(lib().sep_batch_io(self.h, job, C.byref(s), C.byref(o)))
+        return s.value, o.value
+
+    def set_coefficients(self, job, an_re, zn, dE_1, vmin):
+        an_re, zn = _f64(an_re), _f64(zn)
+        _check(lib().sep_batch_set_coefficients(self.h, job, _p(an_re), _p(zn), dE_1, vmin))
+
+    def load_start(self, job, start):
+        start = _f64(start)
+        if start.size != self.ns[job] * self.contexts[job].ngrid:
+            raise ValueError("start must hold ns x ngrid values")
+        _check(lib().sep_batch_load_start(self.h, job, _p(start)))
+
+    def read_out(self, job):
+        out = np.empty((self.ns[job], self.ms, self.contexts[job].ngrid))
+        _check(lib().sep_batch_read_out(self.h, job, _p(out)))
+        return out
+
+    def run(self):
+        _check(lib().sep_batch_run(self.h))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.sep_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

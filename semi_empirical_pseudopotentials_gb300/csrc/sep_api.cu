@@ -523,6 +523,68 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
   return kOk;
 }
 
+int sep_ctx_autotune(sep_ctx* c, long npairs, int reps, int* choices) {
+  RET(check_ctx(c));
+  return autotune_device(c, npairs, reps, choices);
+}
+
+int sep_batch_create(int njobs, sep_ctx* const* ctxs, const long* ns, long ms, long nc,
+                     sep_batch** out) {
+  if (!ctxs || !out) return arg_fail("sep_batch_create: null argument");
+  for (int j = 0; j < njobs; ++j) RET(check_ctx(ctxs[j]));
+  return batch_create(njobs, ctxs, ns, ms, nc, out);
+}
+
+int sep_batch_io(sep_batch* b, int job, double** start_dev, double** out_dev) {
+  if (!b || job < 0 || job >= (int)b->ctx.size()) return arg_fail("sep_batch_io: bad job");
+  if (start_dev) *start_dev = b->start[job];
+  if (out_dev) *out_dev = b->out[job];
+  return kOk;
+}
+
+int sep_batch_set_coefficients(sep_batch* b, int job, const double* an_re, const double* zn,
+                               double dE_1, double vmin) {
+  return batch_set_coefficients(b, job, an_re, zn, dE_1, vmin);
+}
+
+int sep_batch_run(sep_batch* b) { return batch_run(b); }
+
+int sep_batch_load_start(sep_batch* b, int job, const double* host) {
+  if (!b || job < 0 || job >= (int)b->ctx.size() || !host)
+    return arg_fail("sep_batch_load_start: bad argument");
+  CK(cudaMemcpy(b->start[job], host, sizeof(double) * (size_t)b->ns[job] * b->ctx[job]->n,
+                cudaMemcpyHostToDevice));
+  return kOk;
+}
+
+int sep_batch_read_out(sep_batch* b, int job, double* host) {
+  if (!b || job < 0 || job >= (int)b->ctx.size() || !host)
+    return arg_fail("sep_batch_read_out: bad argument");
+  CK(cudaMemcpy(host, b->out[job],
+                sizeof(double) * (size_t)b->ns[job] * b->ms * b->ctx[job]->n,
+                cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+int sep_ctx_set_tiles(sep_ctx* c, const int* choices) {
+  if (!c || !choices) return arg_fail("sep_ctx_set_tiles: null argument");
+  for (int k = 0; k < 5; ++k) {
+    if (choices[k] != 0 && choices[k] != 1) return arg_fail("sep_ctx_set_tiles: shapes are 0 or 1");
+    c->g64.variant[k] = choices[k];
+    c->g32.variant[k] = choices[k];
+  }
+  for (auto& g : c->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return kOk;
+}
+
+int sep_batch_destroy(sep_batch* b) {
+  batch_release(b);
+  delete b;
+  return kOk;
+}
+
 int sep_time_passes(sep_ctx* c, long npairs, int reps, double* ms_out) {
   RET(check_ctx(c));
   if (!ms_out) return arg_fail("sep_time_passes: null argument");

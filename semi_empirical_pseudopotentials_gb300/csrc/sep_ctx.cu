@@ -93,9 +93,14 @@ void drop_graphs(sep_ctx* c) {
   c->graphs.clear();
 }
 
-// grow a workspace buffer; a reallocation invalidates captured graphs
+// grow a workspace buffer; a reallocation invalidates captured graphs.  The
+// filter buffers cannot move while a batch graph refers to them.
 int grow(sep_ctx* c, DevBuf& b, size_t bytes) {
   if (bytes <= b.bytes) return kOk;
+  if (c->batch_holds > 0 && (&b == &c->w_hist || &b == &c->w_fft || &b == &c->w_acc ||
+                             &b == &c->w_coef || &b == &c->w_steps))
+    return arg_fail("the context's filter workspace is held by a batch; destroy the batch or "
+                    "use sizes that fit it");
   cudaStreamSynchronize(c->stream);
   drop_graphs(c);
   cudaError_t e = b.ensure(bytes);
@@ -625,6 +630,204 @@ template <typename T> int time_passes_impl(sep_ctx* c, long npairs, int reps, do
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return kOk;
+}
+
+// Tile-shape autotuner: time both shapes of every pass kind on npairs grids
+// of this context (the filter's precision) and keep the faster.
+template <typename T> int autotune_impl(sep_ctx* c, long npairs, int reps, int* choice) {
+  GridDev<T>& g = Prec<T>::grid(c);
+  const long long n = c->n;
+  RET(grow(c, c->w_hist, sizeof(cx<T>) * (size_t)n * 2 * npairs));
+  RET(grow(c, c->w_fft, sizeof(cx<T>) * (size_t)n * npairs));
+  CK(cudaMemsetAsync(c->w_hist.p, 0, c->w_hist.bytes, c->stream));
+  CK(cudaMemsetAsync(c->w_fft.p, 0, c->w_fft.bytes, c->stream));
+  cx<T>* hist = c->w_hist.as<cx<T>>();
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int axis[5] = {0, 1, 2, 1, 0};
+  const int mode[5] = {kFwd, kFwd, kFwdKInv, kInv, kInvEpiFwd};
+  for (int k = 0; k < 5; ++k) {
+    float best = 1e30f;
+    int arg = 0;
+    for (int v = 0; v < 2; ++v) {
+      PassIO<T> p;
+      p.data = c->w_fft.as<cx<T>>();
+      p.variant = v;
+      if (k == 0) p.src = hist;
+      if (k == 4) {
+        p.psi_in = hist;
+        p.psi_out = hist + (long long)n * npairs;
+      }
+      for (int r = -1; r < reps; ++r) {
+        if (r == 0) CK(cudaEventRecord(e0, c->stream));
+        CK(run_pass<T>(axis[k], mode[k], g, p, (int)npairs, c->stream));
+      }
+      CK(cudaEventRecord(e1, c->stream));
+      CK(cudaEventSynchronize(e1));
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, e0, e1));
+      if (t < best) {
+        best = t;
+        arg = v;
+      }
+    }
+    g.variant[k] = arg;
+    if (choice) choice[k] = arg;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  drop_graphs(c);
+  return kOk;
+}
+
+int autotune_device(sep_ctx* c, long npairs, int reps, int* choice) {
+  if (npairs < 1 || reps < 1) return arg_fail("sep_ctx_autotune: npairs, reps >= 1");
+  if (c->precision == 1) return autotune_impl<float>(c, npairs, reps, choice);
+  return autotune_impl<double>(c, npairs, reps, choice);
+}
+
+// ------------------------------------------------------------------------
+// Batched filter over several contexts (grids): one CUDA graph holds every
+// job's Newton loop as a parallel branch, so a single launch runs them all.
+namespace {
+template <typename T> int batch_job_prepare(sep_ctx* c, long ns, long ms, long nc) {
+  const long long n = c->n;
+  int K = c->block_steps;
+  if (K > nc) K = (int)nc;
+  const long long B = (ns + 1) / 2;
+  RET(grow(c, c->w_hist, sizeof(cx<T>) * (size_t)n * K * B));
+  RET(grow(c, c->w_fft, sizeof(cx<T>) * (size_t)n * B));
+  RET(grow(c, c->w_acc, sizeof(T) * 2 * (size_t)ms * n * B));
+  RET(grow(c, c->w_coef, sizeof(T) * (size_t)ms * nc));
+  RET(grow(c, c->w_steps, sizeof(T) * 2 * (size_t)nc));
+  return kOk;
+}
+
+template <typename T>
+int batch_job_capture(sep_ctx* c, const double* d_start, long ns, long ms, long nc,
+                      double* d_out) {
+  const long long n = c->n;
+  int K = c->block_steps;
+  if (K > nc) K = (int)nc;
+  const int B = (int)((ns + 1) / 2);
+  CK(pack_pairs<T, double>(d_start, ns, n, c->w_hist.as<cx<T>>(), c->stream));
+  RET(newton_loop<T>(c, B, ns, ms, nc, K));
+  if (sizeof(T) == sizeof(double))
+    CK(cudaMemcpyAsync(d_out, c->w_acc.p, sizeof(double) * (size_t)ns * ms * n,
+                       cudaMemcpyDeviceToDevice, c->stream));
+  else
+    CK(convert_f32_to_f64(c->w_acc.as<float>(), d_out, (long long)ns * ms * n, c->stream));
+  return kOk;
+}
+
+template <typename T> int batch_upload(sep_ctx* c, const double* an_re, const double* zn,
+                                       long ms, long nc, double dE_1, double vmin,
+                                       cudaStream_t s) {
+  std::vector<T> a((size_t)ms * nc), st(2 * (size_t)nc, T(0));
+  for (size_t i = 0; i < a.size(); ++i) a[i] = (T)an_re[i];
+  for (long j = 1; j < nc; ++j) {
+    st[2 * j] = (T)dE_1;
+    st[2 * j + 1] = (T)(-(2.0 + zn[j - 1] + vmin * dE_1));
+  }
+  CK(cudaMemcpyAsync(c->w_coef.p, a.data(), sizeof(T) * a.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->w_steps.p, st.data(), sizeof(T) * st.size(), cudaMemcpyHostToDevice,
+                     s));
+  CK(cudaStreamSynchronize(s));
+  return kOk;
+}
+}  // namespace
+
+int batch_create(int njobs, sep_ctx* const* ctxs, const long* ns, long ms, long nc,
+                 sep_batch** out) {
+  if (njobs < 1 || !ctxs || !ns || !out || ms < 1 || ms > 32 || nc < 1)
+    return arg_fail("sep_batch_create: bad argument");
+  for (int j = 0; j < njobs; ++j) {
+    if (!ctxs[j] || ns[j] < 1 || ns[j] > 2 * 65535) return arg_fail("sep_batch_create: bad job");
+    for (int i = 0; i < j; ++i)
+      if (ctxs[i] == ctxs[j]) return arg_fail("sep_batch_create: each job needs its own context");
+  }
+  sep_batch* b = new sep_batch();
+  b->ms = ms;
+  b->nc = nc;
+  auto fail = [&](int r) {
+    delete b;
+    return r;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&b->master, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) return fail(cuda_fail(e, "batch stream", __LINE__));
+  for (int j = 0; j < njobs; ++j) {
+    sep_ctx* c = ctxs[j];
+    b->ctx.push_back(c);
+    b->ns.push_back(ns[j]);
+    double *ds = nullptr, *dout = nullptr;
+    e = cudaMalloc(&ds, sizeof(double) * (size_t)ns[j] * c->n);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, sizeof(double) * (size_t)ns[j] * ms * c->n);
+    b->start.push_back(ds);
+    b->out.push_back(dout);
+    cudaEvent_t ev = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    b->join.push_back(ev);
+    if (e != cudaSuccess) return fail(cuda_fail(e, "batch buffers", __LINE__));
+    int r = (c->precision == 1) ? batch_job_prepare<float>(c, ns[j], ms, nc)
+                                : batch_job_prepare<double>(c, ns[j], ms, nc);
+    if (r != kOk) return fail(r);
+    CK(cudaMemsetAsync(c->w_coef.p, 0, c->w_coef.bytes, c->stream));
+    CK(cudaMemsetAsync(c->w_steps.p, 0, c->w_steps.bytes, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  // capture: master forks to every job's stream, every job joins back
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamBeginCapture(b->master, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(cuda_fail(e, "batch capture", __LINE__));
+  int r = kOk;
+  e = cudaEventRecord(b->fork, b->master);
+  for (int j = 0; j < njobs && e == cudaSuccess && r == kOk; ++j) {
+    sep_ctx* c = b->ctx[j];
+    e = cudaStreamWaitEvent(c->stream, b->fork, 0);
+    if (e != cudaSuccess) break;
+    r = (c->precision == 1)
+            ? batch_job_capture<float>(c, b->start[j], b->ns[j], ms, nc, b->out[j])
+            : batch_job_capture<double>(c, b->start[j], b->ns[j], ms, nc, b->out[j]);
+    if (r != kOk) break;
+    e = cudaEventRecord(b->join[j], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->master, b->join[j], 0);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(b->master, &graph);
+  if (r != kOk) {
+    if (graph) cudaGraphDestroy(graph);
+    return fail(r);
+  }
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(cuda_fail(e, "batch graph", __LINE__));
+  for (sep_ctx* c : b->ctx) c->batch_holds++;
+  *out = b;
+  return kOk;
+}
+
+void batch_release(sep_batch* b) {
+  if (b && b->exec)
+    for (sep_ctx* c : b->ctx) c->batch_holds--;
+}
+
+int batch_set_coefficients(sep_batch* b, int job, const double* an_re, const double* zn,
+                           double dE_1, double vmin) {
+  if (!b || job < 0 || job >= (int)b->ctx.size() || !an_re || !zn)
+    return arg_fail("sep_batch_set_coefficients: bad argument");
+  sep_ctx* c = b->ctx[job];
+  return (c->precision == 1)
+             ? batch_upload<float>(c, an_re, zn, b->ms, b->nc, dE_1, vmin, b->master)
+             : batch_upload<double>(c, an_re, zn, b->ms, b->nc, dE_1, vmin, b->master);
+}
+
+int batch_run(sep_batch* b) {
+  if (!b || !b->exec) return arg_fail("sep_batch_run: no batch");
+  CK(cudaGraphLaunch(b->exec, b->master));
+  CK(cudaStreamSynchronize(b->master));
   return kOk;
 }
 

@@ -37,6 +37,29 @@ struct FilterGraph {
 
 }  // namespace sep
 
+struct sep_ctx;
+
+// a set of jobs (one context each) whose Newton loops form one CUDA graph
+struct sep_batch {
+  std::vector<sep_ctx*> ctx;
+  std::vector<long> ns;
+  long ms = 0, nc = 0;
+  std::vector<double*> start, out;
+  cudaStream_t master = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t exec = nullptr;
+  ~sep_batch() {
+    if (master) cudaStreamSynchronize(master);
+    if (exec) cudaGraphExecDestroy(exec);
+    for (double* p : start) cudaFree(p);
+    for (double* p : out) cudaFree(p);
+    for (cudaEvent_t e : join) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (master) cudaStreamDestroy(master);
+  }
+};
+
 struct sep_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -49,6 +72,7 @@ struct sep_ctx {
   bool have_pot = false;
   bool use_graphs = true;
   int block_steps = 32;
+  int batch_holds = 0;  // batches whose graph points at the filter workspace
   sep::host::KTables ktab;
   sep::GridDev<double> g64;
   sep::GridDev<float> g32;
@@ -72,5 +96,12 @@ int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host);
 int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host);
 int normalize_device(sep_ctx* c, double* d_psi, long m);
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out);
+int autotune_device(sep_ctx* c, long npairs, int reps, int* choice);
+int batch_create(int njobs, sep_ctx* const* ctxs, const long* ns, long ms, long nc,
+                 sep_batch** out);
+int batch_set_coefficients(sep_batch* b, int job, const double* an_re, const double* zn,
+                           double dE_1, double vmin);
+int batch_run(sep_batch* b);
+void batch_release(sep_batch* b);
 
 }  // namespace sep

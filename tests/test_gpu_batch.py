@@ -1,0 +1,65 @@
+"""Many nanocrystals in one graph launch, and the tile-shape autotuner.
+
+A batch runs each job's Newton loop as a branch of one CUDA graph: every job's
+output must equal that job run alone through sep_filter, bit for bit.  The two
+compiled tile shapes split the lines over blocks differently but do the same
+arithmetic per line, so the autotuner's choice must not change any result."""
+import numpy as np
+import pytest
+
+import semi_empirical_pseudopotentials_gb300 as sep
+
+pytestmark = pytest.mark.gpu
+
+
+def _job(dims, seed, precision):
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(dims))
+    steps = (0.9, 0.85, 0.8)
+    pot = -1.5 * np.exp(-rng.uniform(0.5, 1.5) * np.linspace(-2, 2, n) ** 2)
+    ctx = sep.Context(dims, steps, potl=pot, precision=precision)
+    dv = steps[0] * steps[1] * steps[2]
+    return ctx, pot, dv, n
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_batch_equals_single_runs(precision):
+    shapes = [(32, 32, 32), (36, 40, 48), (48, 48, 48)]
+    ns, ms, nc = [3, 4, 2], 3, 40
+    jobs = [_job(d, i, precision) for i, d in enumerate(shapes)]
+    dE = 40.0
+    singles, coefs = [], []
+    for (ctx, pot, dv, n), s in zip(jobs, ns):
+        vmin = float(pot.min())
+        ar, ai, zn = sep.coefficients([-1.2, -0.8, -0.4], nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+        start = sep.start_states(-17 - s, s, n, dv)
+        singles.append((start, ctx.filter(start, ar, zn, 4.0 / dE, vmin)))
+        coefs.append((ar, zn, vmin))
+    b = sep.Batch([j[0] for j in jobs], ns, ms, nc)
+    for k, (ar, zn, vmin) in enumerate(coefs):
+        b.set_coefficients(k, ar, zn, 4.0 / dE, vmin)
+        b.load_start(k, singles[k][0])
+    b.run()
+    for k in range(len(jobs)):
+        assert np.array_equal(b.read_out(k), singles[k][1]), k
+    b.run()  # the same graph again
+    assert np.array_equal(b.read_out(2), singles[2][1])
+    b.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_autotuned_tile_shapes_give_identical_results(precision):
+    dims = (64, 64, 64)
+    ctx, pot, dv, n = _job(dims, 7, precision)
+    vmin = float(pot.min())
+    nc, dE = 33, 40.0
+    ar, ai, zn = sep.coefficients([-1.0, -0.5], nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+    start = sep.start_states(-5, 6, n, dv)
+    a = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    ctx.set_tiles([1, 1, 1, 1, 1])
+    b = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    assert np.array_equal(a, b)
+    choice = ctx.autotune(3, reps=3)
+    assert len(choice) == 5 and set(choice) <= {0, 1}
+    c = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    assert np.array_equal(a, c)
