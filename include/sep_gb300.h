@@ -214,6 +214,30 @@ int sep_ctx_set_tiles(sep_ctx *ctx, const int *choices);
  * reference; used for the roofline report. */
 int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
 
+/* ---- normalisation that allocates nothing ------------------------------
+ * filter/norm.c:40-54 (psi_m <- psi_m / sqrt(dv sum_g psi_m(g)^2)) on m real
+ * states of ngrid doubles already on the device, psi_dev state-major.  No
+ * counterpart in the reference (which normalises host arrays, and whose
+ * drop-in here, sep_normalize_states, copies them to the device and
+ * allocates on each call).  This one calls no cudaMalloc/cudaFree or any
+ * other allocating routine, for callers that cannot allocate at that point:
+ * code running while another allocator (a framework's caching pool) holds
+ * the device's memory, and loops that must not wait on cudaMalloc/cudaFree.
+ *  - Scratch: a fixed 2,105,344-byte array in the library's device image (one
+ *    per device); nothing in it needs to start at zero.
+ *  - Limit: m <= 1024 states per call (SEP_ERR_ARG above that; split the
+ *    block).  ngrid is not limited.
+ *  - Device: the calling thread's current device; psi_dev must live there.
+ *    The first call on each device looks up the scratch address there
+ *    (cudaGetSymbolAddress); make that first call before any stream capture
+ *    begins.
+ *  - Asynchronous on cuda_stream (a cudaStream_t; NULL = the legacy default
+ *    stream): the states are normalised when the stream reaches the call.
+ *  - Calls that overlap on one device (other streams or threads, not
+ *    ordered by the caller) share the scratch and race: serialise them. */
+int sep_normalize_states_noalloc(double *psi_dev, long m, long ngrid, double dv,
+                                 void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
