@@ -99,6 +99,14 @@ def tables(sep, S):
     return tr, tv
 
 
+# ncu dram__bytes_read.sum + dram__bytes_write.sum per pair, 128^3 complex64,
+# from the 12-pair capture summarised in profiles/line_pass_c64_128.md
+TRAFFIC_PER_PAIR_128 = {"y_fwd": (201.354752e6 + 142.915584e6) / 12,
+                        "z_fki": (201.357312e6 + 140.684032e6) / 12,
+                        "y_inv": (201.346304e6 + 143.166208e6) / 12,
+                        "x_inv_epi_fwd": (444.561152e6 + 351.911936e6) / 12}
+
+
 def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):
     """Compulsory HBM bytes of one launch (c: bytes per complex, r: per real)."""
     if kind in ("x_fwd", "y_fwd", "z_fki", "y_inv"):
@@ -367,11 +375,13 @@ def run_sep(args):
         k = int(np.argmax(share))
         byts = algorithmic_bytes(names[k], npairs, n, 8, 4)
         achieved = byts / (per[k] * 1e-3) / 1e9
+        # DRAM bytes (read + write) per pair per launch from one ncu capture of
+        # the 128^3 complex64 passes on 12 pairs (profiles/line_pass_c64_128.md),
+        # scaled to this launch's pairs: traffic grows in proportion to the pairs.
         traffic = None
-        tf = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
-        if os.path.exists(tf):
-            with open(tf) as f:
-                traffic = json.load(f).get("mixed_128", {}).get(names[k])
+        per_pair = TRAFFIC_PER_PAIR_128.get(names[k])
+        if per_pair is not None and tuple(S.dims) == (128, 128, 128):
+            traffic = per_pair * npairs
         extras["roofline"] = {
             "bound": "hbm", "kernel": names[k], "achieved": achieved,
             "peak": peaks.get("hbm_gbs"), "unit": "GB/s",

@@ -177,6 +177,31 @@ int sep_vbuild_backward(sep_ctx *ctx, long natom, const double *xyz, const int *
  * counterpart in the reference (it has no gradients). */
 int sep_hf_density(sep_ctx *ctx, const double *psi, long m, const double *w, double *rho);
 
+/* ---- band-edge adjoint: forward and backward ------------------------------
+ * theta = a0..a3 per type (ntype x 4, pseudopotFitting/hamiltonian.c:91-94).
+ * No counterpart in the reference, which fits theta by a derivative-free
+ * Monte Carlo search (pseudopotFitting/fit.c:29-50).
+ *
+ * Forward, step 1: the 1024-point table of each type (pot.c:35-63), minus its
+ * last value (filter/read.c:105-108), then V(r) on the context grid
+ * (filter/init.c:157-182), installed as the context's potential (potl: host
+ * copy, may be NULL).  Step 2 is sep_pipeline on that potential. */
+int sep_potential_from_params(sep_ctx *ctx, long natom, const double *xyz, const int *types,
+                              const double *scale, long ntype, const double *params,
+                              double vol_per_atom, const double mins[3], double *potl);
+/* Backward: dparams (ntype x 4) = dL/dtheta for Ritz pairs (psi: m x ngrid
+ * normalised states of the last forward, host) and dL_dE (m).  Chain:
+ * Hellmann-Feynman density, V(r) backward, adjoint of the table shift,
+ * transpose of the sine-transform Jacobian. */
+int sep_band_edge_backward(sep_ctx *ctx, long natom, const double *xyz, const int *types,
+                           const double *scale, long ntype, const double *params,
+                           double vol_per_atom, const double mins[3], const double *psi, long m,
+                           const double *dL_dE, double *dparams);
+/* The table part of the backward for one type: dparams[4] from dL/d(shifted
+ * table) (1024 values).  Host only. */
+int sep_form_factor_backward(const double params[4], double vol_per_atom, const double *dtab,
+                             double *dparams);
+
 /* ---- many nanocrystals in one launch ---------------------------------------
  * A batch holds one job per context (grids may differ): job j filters ns[j]
  * start states with ms targets and nc Newton steps.  sep_batch_create
@@ -204,6 +229,20 @@ int sep_batch_destroy(sep_batch *b);
 int sep_ctx_autotune(sep_ctx *ctx, long npairs, int reps, int *choices);
 /* Set the 5 tile shapes (0 or 1) by hand. */
 int sep_ctx_set_tiles(sep_ctx *ctx, const int *choices);
+
+/* ---- subspace contractions ------------------------------------------------
+ * The Gram, projection and rotation products of sep_ortho (filter/ortho.c:11-52)
+ * and sep_rayleigh_ritz (filter/Hmat.c:11-86).  mode 1 (default): on the
+ * tcgen05 tensor cores by exact splitting into bf16 digits with exact integer
+ * accumulation, FP64-accurate; mode 0: on the FP64 pipe. */
+int sep_ctx_set_subspace(sep_ctx *ctx, int mode);
+/* C (m x n) = alpha A B^T, A m x k, B n x k (host, row-major); sym: B = A
+ * (B may be NULL) and C is symmetric.  Uses the context's mode. */
+int sep_subspace_gemm(sep_ctx *ctx, const double *A, const double *B, long m, long n, long k,
+                      double alpha, int sym, double *C);
+/* out (m x w) = W (m x k) X (k x w), host row-major.  Uses the context's mode. */
+int sep_subspace_rotate(sep_ctx *ctx, const double *W, const double *X, long m, long k, long w,
+                        double *out);
 
 /* ---- measurement --------------------------------------------------------
  * Average device time (ms, CUDA events on the context stream) of one launch

@@ -91,6 +91,15 @@ def lib():
         L.sep_batch_load_start.argtypes = [vp, C.c_int, dp]
         L.sep_batch_read_out.argtypes = [vp, C.c_int, dp]
         L.sep_ctx_set_tiles.argtypes = [vp, ip]
+        L.sep_form_factor_backward.argtypes = [dp, C.c_double, dp, dp]
+        L.sep_ctx_set_subspace.argtypes = [vp, C.c_int]
+        L.sep_subspace_gemm.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, C.c_double,
+                                        C.c_int, dp]
+        L.sep_subspace_rotate.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, dp]
+        L.sep_potential_from_params.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, C.c_double,
+                                                dp, dp]
+        L.sep_band_edge_backward.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, C.c_double,
+                                             dp, dp, C.c_long, dp, dp]
         _lib = L
     return _lib
 
@@ -145,6 +154,16 @@ def form_factor_table(params, vol_per_atom):
     r, v = np.empty(1024), np.empty(1024)
     _check(lib().sep_form_factor_table(_p(a), vol_per_atom, _p(r), _p(v)))
     return r, v
+
+
+def form_factor_backward(params, vol_per_atom, dtab):
+    """dL/da0..a3 from dL/d(shifted 1024-point table), host only."""
+    a, d = _f64(params), _f64(dtab)
+    if d.shape != (1024,):
+        raise ValueError("dtab must hold 1024 values")
+    g = np.empty(4)
+    _check(lib().sep_form_factor_backward(_p(a), vol_per_atom, _p(d), _p(g)))
+    return g
 
 
 class Context:
@@ -331,6 +350,59 @@ class Context:
                                 _p(tab_v), tab_n.ctypes.data_as(lp), tab_r.shape[1], _p(mins),
                                 _p(out), 1 if install else 0))
         return out
+
+    def set_subspace(self, mode):
+        """Subspace contractions on the tensor cores ("tc", default) or the FP64 pipe ("f64")."""
+        _check(lib().sep_ctx_set_subspace(self.h, {"f64": 0, "tc": 1}[mode]))
+
+    def subspace_gemm(self, A, B=None, alpha=1.0):
+        """alpha A B^T through the context's subspace contraction (B None: A A^T)."""
+        A = _f64(A)
+        sym = B is None
+        Bm = A if sym else _f64(B)
+        if Bm.shape[1] != A.shape[1]:
+            raise ValueError("A and B need the same number of columns")
+        out = np.empty((A.shape[0], Bm.shape[0]))
+        _check(lib().sep_subspace_gemm(self.h, _p(A), None if sym else _p(Bm), A.shape[0],
+                                       Bm.shape[0], A.shape[1], alpha, 1 if sym else 0, _p(out)))
+        return out
+
+    def subspace_rotate(self, W, X):
+        """W X through the context's subspace contraction."""
+        W, X = _f64(W), _f64(X)
+        if W.shape[1] != X.shape[0]:
+            raise ValueError("inner dimensions differ")
+        out = np.empty((W.shape[0], X.shape[1]))
+        _check(lib().sep_subspace_rotate(self.h, _p(W), _p(X), W.shape[0], W.shape[1],
+                                         X.shape[1], _p(out)))
+        return out
+
+    def potential_from_params(self, xyz, types, params, vol_per_atom, mins, scale=None):
+        """Shifted form-factor tables of theta (ntype x 4), then V(r), installed."""
+        xyz, th, mins = _f64(xyz), _f64(params).reshape(-1, 4), _f64(mins)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        sc = None if scale is None else _f64(scale)
+        out = np.empty(self.ngrid)
+        _check(lib().sep_potential_from_params(self.h, len(xyz), _p(xyz), types.ctypes.data_as(ip),
+                                               None if sc is None else _p(sc), th.shape[0],
+                                               _p(th), vol_per_atom, _p(mins), _p(out)))
+        return out
+
+    def band_edge_backward(self, xyz, types, params, vol_per_atom, mins, psi, dL_dE, scale=None):
+        """dL/dtheta (ntype x 4) for Ritz states psi (m x ngrid) and dL/dE (m)."""
+        xyz, th, mins = _f64(xyz), _f64(params).reshape(-1, 4), _f64(mins)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        sc = None if scale is None else _f64(scale)
+        psi = _f64(psi).reshape(-1, self.ngrid)
+        w = _f64(dL_dE)
+        if len(w) != psi.shape[0]:
+            raise ValueError("one dL/dE per state")
+        g = np.empty_like(th)
+        _check(lib().sep_band_edge_backward(self.h, len(xyz), _p(xyz), types.ctypes.data_as(ip),
+                                            None if sc is None else _p(sc), th.shape[0], _p(th),
+                                            vol_per_atom, _p(mins), _p(psi), psi.shape[0], _p(w),
+                                            _p(g)))
+        return g
 
     def vbuild_backward(self, xyz, types, tab_r, tab_v, tab_n, mins, dpotl, scale=None):
         xyz = _f64(xyz)

@@ -25,8 +25,9 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 CUDA_UNITS = ["sep_pass_f64.cu", "sep_pass_f32.cu", "sep_pass_f64_v1.cu", "sep_pass_f32_v1.cu",
               "sep_kernels.cu", "sep_ctx.cu",
-              "sep_api.cu", "sep_vbuild.cu", "sep_noalloc.cu"]
-CXX_UNITS = ["sep_host.cpp"]
+              "sep_api.cu", "sep_vbuild.cu", "sep_noalloc.cu",
+              "sep_ozaki.cu"]
+CXX_UNITS = ["sep_host.cpp", "sep_adjoint.cpp"]
 
 
 def cuda_home():

@@ -127,7 +127,8 @@ sep_ctx::~sep_ctx() {
   free_grid(g64);
   free_grid(g32);
   for (DevBuf* b : {&w_hist, &w_fft, &w_acc, &w_coef, &w_steps, &w_start, &w_out, &w_red,
-                    &w_small, &w_states, &w_states2, &w_tmp, &w_solver, &w_gemm, &w_hpsi})
+                    &w_small, &w_states, &w_states2, &w_tmp, &w_solver, &w_gemm, &w_hpsi,
+                    &w_ozA, &w_ozB, &w_ozP, &w_ozE})
     b->release();
   if (solver) cusolverDnDestroy(solver);
   if (stream) cudaStreamDestroy(stream);
@@ -589,6 +590,65 @@ int sep_time_passes(sep_ctx* c, long npairs, int reps, double* ms_out) {
   RET(check_ctx(c));
   if (!ms_out) return arg_fail("sep_time_passes: null argument");
   return time_passes_device(c, npairs, reps, ms_out);
+}
+
+int sep_ctx_set_subspace(sep_ctx* c, int mode) {
+  if (!c || (mode != 0 && mode != 1)) return arg_fail("sep_ctx_set_subspace: mode is 0 or 1");
+  c->subspace_tc = mode;
+  return kOk;
+}
+
+namespace {
+// device copies of host operands for the two subspace entry points below
+struct Tmp {
+  std::vector<double*> p;
+  ~Tmp() {
+    for (double* q : p) cudaFree(q);
+  }
+  cudaError_t get(size_t count, double** out) {
+    double* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(double) * (count ? count : 1));
+    if (e == cudaSuccess) p.push_back(q);
+    *out = q;
+    return e;
+  }
+};
+}  // namespace
+
+int sep_subspace_gemm(sep_ctx* c, const double* A, const double* B, long m, long n, long k,
+                      double alpha, int sym, double* C) {
+  RET(check_ctx(c, false));
+  if (!A || !C || (!sym && !B) || m < 1 || n < 1 || k < 1 || (sym && m != n))
+    return arg_fail("sep_subspace_gemm: bad argument");
+  Tmp t;
+  double *dA, *dB = nullptr, *dC;
+  CK(t.get((size_t)m * k, &dA));
+  if (!sym) CK(t.get((size_t)n * k, &dB));
+  CK(t.get((size_t)m * n, &dC));
+  CK(cudaMemcpyAsync(dA, A, sizeof(double) * m * k, cudaMemcpyHostToDevice, c->stream));
+  if (!sym) CK(cudaMemcpyAsync(dB, B, sizeof(double) * n * k, cudaMemcpyHostToDevice, c->stream));
+  RET(subspace_gemm_device(c, dA, sym ? dA : dB, m, n, k, alpha, sym != 0, dC));
+  CK(cudaMemcpyAsync(C, dC, sizeof(double) * m * n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return kOk;
+}
+
+int sep_subspace_rotate(sep_ctx* c, const double* W, const double* X, long m, long k, long w,
+                        double* out) {
+  RET(check_ctx(c, false));
+  if (!W || !X || !out || m < 1 || k < 1 || w < 1)
+    return arg_fail("sep_subspace_rotate: bad argument");
+  Tmp t;
+  double *dW, *dX, *dO;
+  CK(t.get((size_t)m * k, &dW));
+  CK(t.get((size_t)k * w, &dX));
+  CK(t.get((size_t)m * w, &dO));
+  CK(cudaMemcpyAsync(dW, W, sizeof(double) * m * k, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(dX, X, sizeof(double) * k * w, cudaMemcpyHostToDevice, c->stream));
+  RET(subspace_rotate_device(c, dW, dX, m, k, w, dO));
+  CK(cudaMemcpyAsync(out, dO, sizeof(double) * m * w, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return kOk;
 }
 
 // ---- host helpers --------------------------------------------------------

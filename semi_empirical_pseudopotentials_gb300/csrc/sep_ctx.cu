@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "sep_ctx.cuh"
+#include "sep_ozaki.cuh"
 
 namespace sep {
 
@@ -290,6 +291,95 @@ int syevd(sep_ctx* c, double* d_a, long long m, double* d_w) {
   return kOk;
 }
 
+// ---- subspace contractions --------------------------------------------------
+// On the tensor cores by exact splitting (sep_ozaki.cuh) when c->subspace_tc,
+// else on the FP64 pipe.  Both give FP64-accurate products.
+constexpr double kSliceBudgetBytes = 4.0e9;  // slice planes held per contraction pass
+
+struct OzSpace {
+  oz::Planes A, B;
+  long long* part = nullptr;
+  int* err = nullptr;
+};
+
+// workspace for operands of up to rowsA / rowsB rows and kk values of K
+int oz_space(sep_ctx* c, long long rowsA, long long rowsB, long long kk, bool same, int nsplit,
+             OzSpace& w) {
+  const size_t ea = oz::plane_elems(rowsA, kk);
+  const size_t eb = same ? 0 : oz::plane_elems(rowsB, kk);
+  RET(grow(c, c->w_ozA, 2 * ea));
+  if (!same) RET(grow(c, c->w_ozB, 2 * eb));
+  RET(grow(c, c->w_ozP, 8 * (oz::part_elems(rowsA, rowsB, nsplit) + 8)));
+  const size_t ne = 64 + (size_t)(rowsA + rowsB) + 512;
+  RET(grow(c, c->w_ozE, sizeof(int) * ne));
+  int* e = c->w_ozE.as<int>();
+  CK(cudaMemsetAsync(e, 0, sizeof(int), c->stream));
+  w.err = e;
+  w.A.d = c->w_ozA.as<uint16_t>();
+  w.A.expo = e + 64;
+  w.B.d = same ? w.A.d : c->w_ozB.as<uint16_t>();
+  w.B.expo = same ? w.A.expo : e + 64 + (rowsA + 256);
+  w.part = c->w_ozP.as<long long>();
+  return kOk;
+}
+
+int oz_check(sep_ctx* c) {
+  if (!c->subspace_tc || !c->w_ozE.p) return kOk;
+  int h = 0;
+  CK(oz::check_status(c->w_ozE.as<int>(), c->stream, &h));
+  if (h != 0) {
+    char b[160];
+    snprintf(b, sizeof b, "tensor-core contraction: a bounded wait in the kernel ran out (%d)", h);
+    set_error(b);
+    CK(cudaMemsetAsync(c->w_ozE.p, 0, sizeof(int), c->stream));
+    return kErrCuda;
+  }
+  return kOk;
+}
+
+// C (M x Nn, dense) = alpha A B^T, A (M x K) and B (Nn x K) with rows K apart;
+// sym: A == B, the symmetric result is mirrored
+int sub_gemm_nt(sep_ctx* c, const double* A, const double* B, long long M, long long Nn,
+                long long K, double alpha, double* C, bool sym) {
+  if (!c->subspace_tc) {
+    const size_t wd = gemm_nt_work_doubles(M, Nn, K);
+    RET(grow(c, c->w_gemm, sizeof(double) * wd));
+    CK(gemm_nt_f64(A, B, M, Nn, K, alpha, C, sym, c->w_gemm.as<double>(), wd, c->stream));
+    return kOk;
+  }
+  const bool same = sym || A == B;
+  const long long rows = (M + 127) / 128 * 128 + (same ? 0 : (Nn + 127) / 128 * 128);
+  long long kc = (long long)(kSliceBudgetBytes / (double)(rows * oz::kSlices * 2));
+  kc = std::max<long long>(oz::kDrainK, kc / oz::kDrainK * oz::kDrainK);
+  kc = std::min<long long>(kc, (K + oz::kChunkK - 1) / oz::kChunkK * oz::kChunkK);
+  const int nsplit = oz::choose_splits(M, Nn, kc, sym);
+  OzSpace w;
+  RET(oz_space(c, M, Nn, kc, same, nsplit, w));
+  for (long long k0 = 0; k0 < K; k0 += kc) {
+    const long long kw = std::min<long long>(kc, K - k0);
+    CK(oz::slice_rows(A + k0, M, kw, K, w.A, c->stream));
+    if (!same) CK(oz::slice_rows(B + k0, Nn, kw, K, w.B, c->stream));
+    else w.B = w.A;
+    CK(oz::gemm_nt(w.A, w.B, alpha, sym, k0 > 0, C, Nn, w.part, nsplit, w.err, c->stream));
+  }
+  return oz_check(c);
+}
+
+// C (M x w, dense) = W (M x K, dense) * X[0:K, 0:w] (rows of X ldx apart)
+int sub_gemm_nn_ld(sep_ctx* c, const double* W, const double* X, long long M, long long w,
+                   long long K, long long ldx, double* C) {
+  if (!c->subspace_tc) {
+    CK(gemm_nn_f64_ld(W, X, M, w, K, ldx, C, c->stream));
+    return kOk;
+  }
+  OzSpace s;
+  RET(oz_space(c, M, w, K, false, 1, s));
+  CK(oz::slice_rows(W, M, K, K, s.A, c->stream));
+  CK(oz::slice_cols(X, K, w, ldx, s.B, c->stream));
+  CK(oz::gemm_nt(s.A, s.B, 1.0, false, false, C, w, nullptr, 1, s.err, c->stream));
+  return kOk;
+}
+
 // rows of psi (m x n) <- W (k x m) psi, in place over column chunks
 int rotate_rows(sep_ctx* c, double* d_psi, long long m, long long k, const double* d_w) {
   const long long n = c->n;
@@ -301,11 +391,11 @@ int rotate_rows(sep_ctx* c, double* d_psi, long long m, long long k, const doubl
   for (long long g0 = 0; g0 < n; g0 += cols) {
     const long long w = std::min<long long>(cols, n - g0);
     // out_chunk (k x w) = W (k x m) * psi[:, g0:g0+w] (m x w, leading dim n)
-    CK(gemm_nn_f64_ld(d_w, d_psi + g0, k, w, m, n, c->w_tmp.as<double>(), c->stream));
+    RET(sub_gemm_nn_ld(c, d_w, d_psi + g0, k, w, m, n, c->w_tmp.as<double>()));
     CK(cudaMemcpy2DAsync(d_psi + g0, sizeof(double) * n, c->w_tmp.p, sizeof(double) * w,
                          sizeof(double) * w, k, cudaMemcpyDeviceToDevice, c->stream));
   }
-  return kOk;
+  return oz_check(c);
 }
 
 }  // namespace
@@ -425,11 +515,11 @@ int rotate_into(sep_ctx* c, const double* d_psi, long long m, long long k, const
   RET(grow(c, c->w_tmp, sizeof(double) * (size_t)k * cols));
   for (long long g0 = 0; g0 < n; g0 += cols) {
     const long long w = std::min<long long>(cols, n - g0);
-    CK(gemm_nn_f64_ld(d_w, d_psi + g0, k, w, m, n, c->w_tmp.as<double>(), c->stream));
+    RET(sub_gemm_nn_ld(c, d_w, d_psi + g0, k, w, m, n, c->w_tmp.as<double>()));
     CK(cudaMemcpy2DAsync(d_out + g0, sizeof(double) * n, c->w_tmp.p, sizeof(double) * w,
                          sizeof(double) * w, k, cudaMemcpyDeviceToDevice, c->stream));
   }
-  return kOk;
+  return oz_check(c);
 }
 
 // x (m x n) -= P^T Q with P = Q x^T dv (k x m): removes span(Q) from the rows of x
@@ -438,17 +528,18 @@ int project_out(sep_ctx* c, double* d_x, long long m, const double* d_q, long lo
   const long long n = c->n;
   const size_t wd = gemm_nt_work_doubles(k, m, n);
   RET(grow(c, c->w_gemm, sizeof(double) * wd));
-  CK(gemm_nt_f64(d_q, d_x, k, m, n, c->dv, P, false, c->w_gemm.as<double>(), wd, c->stream));
+  (void)wd;
+  RET(sub_gemm_nt(c, d_q, d_x, k, m, n, c->dv, P, false));
   CK(transpose_f64(P, k, m, Pt, c->stream));  // Pt: m x k
   long long cols = (long long)((size_t)1 << 27) / (sizeof(double) * std::max<long long>(m, 1));
   cols = std::max<long long>(64, std::min<long long>(cols, n));
   RET(grow(c, c->w_tmp, sizeof(double) * (size_t)m * cols));
   for (long long g0 = 0; g0 < n; g0 += cols) {
     const long long w = std::min<long long>(cols, n - g0);
-    CK(gemm_nn_f64_ld(Pt, d_q + g0, m, w, k, n, c->w_tmp.as<double>(), c->stream));
+    RET(sub_gemm_nn_ld(c, Pt, d_q + g0, m, w, k, n, c->w_tmp.as<double>()));
     CK(sub_2d_f64(d_x + g0, n, c->w_tmp.as<double>(), m, w, c->stream));
   }
-  return kOk;
+  return oz_check(c);
 }
 
 // Loewdin: rows of x (k x n) <- (x x^T dv)^-1/2 x, in place
@@ -457,7 +548,8 @@ int loewdin(sep_ctx* c, double* d_x, long long k, double* G, double* lam, double
   const long long n = c->n;
   const size_t wd = gemm_nt_work_doubles(k, k, n);
   RET(grow(c, c->w_gemm, sizeof(double) * wd));
-  CK(gemm_nt_f64(d_x, d_x, k, k, n, c->dv, G, true, c->w_gemm.as<double>(), wd, c->stream));
+  (void)wd;
+  RET(sub_gemm_nt(c, d_x, d_x, k, k, n, c->dv, G, true));
   RET(syevd(c, G, k, lam));
   // (x x^T dv)^-1/2 = V diag(lam^-1/2) V^T; the column-major eigenvector
   // buffer read row-major is R = V^T, so the factor is R^T (diag(lam^-1/2) R)
@@ -482,8 +574,8 @@ int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept) {
   double* Q = c->w_states2.as<double>();
   const size_t wd = gemm_nt_work_doubles(m, m, n);
   RET(grow(c, c->w_gemm, sizeof(double) * wd));
-  CK(gemm_nt_f64(d_psi, d_psi, m, m, n, c->dv, G, true, c->w_gemm.as<double>(), wd,
-                 c->stream));
+  (void)wd;
+  RET(sub_gemm_nt(c, d_psi, d_psi, m, m, n, c->dv, G, true));
   RET(syevd(c, G, m, lam));
   std::vector<double> hl(m);
   CK(cudaMemcpyAsync(hl.data(), lam, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
@@ -506,8 +598,7 @@ int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept) {
     // level 2 on the remainder of psi
     RET(project_out(c, d_psi, m, Q, k1, P, Pt));
     RET(project_out(c, d_psi, m, Q, k1, P, Pt));
-    CK(gemm_nt_f64(d_psi, d_psi, m, m, n, c->dv, G, true, c->w_gemm.as<double>(), wd,
-                   c->stream));
+    RET(sub_gemm_nt(c, d_psi, d_psi, m, m, n, c->dv, G, true));
     RET(syevd(c, G, m, lam));
     CK(cudaMemcpyAsync(hl.data(), lam, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -547,8 +638,8 @@ int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host) {
   for (long long r0 = 0; r0 < m; r0 += chunk) {
     const long long rc = std::min<long long>(chunk, m - r0);
     RET(apply_h_real(c, d_psi + r0 * n, hps, rc));
-    CK(gemm_nt_f64(hps, d_psi, rc, m, n, c->dv, A + r0 * m, false, c->w_gemm.as<double>(), wd,
-                   c->stream));
+    (void)wd;
+    RET(sub_gemm_nt(c, hps, d_psi, rc, m, n, c->dv, A + r0 * m, false));
   }
   (void)At;
   CK(symmetrize_f64(A, m, c->stream));
@@ -829,6 +920,19 @@ int batch_run(sep_batch* b) {
   CK(cudaGraphLaunch(b->exec, b->master));
   CK(cudaStreamSynchronize(b->master));
   return kOk;
+}
+
+// C (m x n) = alpha A B^T and out (m x w) = W X through the subspace
+// contraction path of the context (device pointers, dense row-major)
+int subspace_gemm_device(sep_ctx* c, const double* A, const double* B, long long m, long long n,
+                         long long k, double alpha, bool sym, double* C) {
+  return sub_gemm_nt(c, A, sym ? A : B, m, n, k, alpha, C, sym);
+}
+
+int subspace_rotate_device(sep_ctx* c, const double* W, const double* X, long long m,
+                           long long k, long long w, double* out) {
+  RET(sub_gemm_nn_ld(c, W, X, m, w, k, w, out));
+  return oz_check(c);
 }
 
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out) {

@@ -72,13 +72,14 @@ struct sep_ctx {
   bool have_pot = false;
   bool use_graphs = true;
   int block_steps = 32;
+  int subspace_tc = 1;  // subspace contractions on the tensor cores (1) or the FP64 pipe (0)
   int batch_holds = 0;  // batches whose graph points at the filter workspace
   sep::host::KTables ktab;
   sep::GridDev<double> g64;
   sep::GridDev<float> g32;
   // workspace
   sep::DevBuf w_hist, w_fft, w_acc, w_coef, w_steps, w_start, w_out, w_red, w_small,
-      w_states, w_states2, w_tmp, w_solver, w_gemm, w_hpsi;
+      w_states, w_states2, w_tmp, w_solver, w_gemm, w_hpsi, w_ozA, w_ozB, w_ozP, w_ozE;
   std::vector<sep::FilterGraph> graphs;
   ~sep_ctx();
 };
@@ -96,6 +97,10 @@ int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host);
 int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host);
 int normalize_device(sep_ctx* c, double* d_psi, long m);
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out);
+int subspace_gemm_device(sep_ctx* c, const double* A, const double* B, long long m, long long n,
+                         long long k, double alpha, bool sym, double* C);
+int subspace_rotate_device(sep_ctx* c, const double* W, const double* X, long long m,
+                           long long k, long long w, double* out);
 int autotune_device(sep_ctx* c, long npairs, int reps, int* choice);
 int batch_create(int njobs, sep_ctx* const* ctxs, const long* ns, long ms, long nc,
                  sep_batch** out);

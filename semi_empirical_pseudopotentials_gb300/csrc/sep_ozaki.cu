@@ -1,0 +1,630 @@
+// sep_ozaki.cu -- exact-split FP64 contractions on the tcgen05 tensor cores
+// (see sep_ozaki.cuh for the arithmetic).
+//
+// Kernel shape (k_oz_mma): one CTA per SM, 256 threads, persistent over work
+// items (an output tile of 128 x 64 and a range of K).  Thread 0 issues the
+// bulk copies (cp.async.bulk, mbarrier transaction counts) of the pre-tiled
+// slice blocks and the tcgen05.mma instructions; the accumulators of the
+// kSlices levels live in TMEM (kSlices x 64 FP32 columns of 128 lanes); every
+// kDrainK of K the eight warps read them back with tcgen05.ld (warp w: lanes
+// 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31 of each level) and add them
+// into two int64 fixed-point registers per output element: levels 0-3 in
+// units of 2^-24 of level 0, levels 4-6 in units of 2^-48.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "sep_ozaki.cuh"
+
+namespace sep {
+namespace oz {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kStages = 2;
+constexpr int kSliceA = kTileM * kChunkK * 2;               // 8192 bytes
+constexpr int kSliceB = kTileN * kChunkK * 2;               // 4096 bytes
+constexpr int kStageBytes = kSlices * (kSliceA + kSliceB);  // 86016 bytes
+constexpr int kTmemCols = 512;                              // kSlices * 64 = 448 used
+constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 4
+constexpr long long kSpin = 1LL << 26;                      // bounded waits
+static_assert(kSlices * kTileN <= kTmemCols, "TMEM columns");
+static_assert((kSlices) * kDrainK * 16384LL < (1LL << 24), "exact FP32 level sums");
+
+// ---- PTX wrappers ----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+// true once the barrier's phase with the given parity has completed
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; false (and *err set) if the phase never completes
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  for (long long it = 0; it < kSpin; ++it)
+    if (mbar_try(bar, parity)) return true;
+  atomicCAS(err, 0, code);
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// shared memory matrix descriptor: K-major, no swizzle; LBO = byte distance of
+// core matrices along K, SBO = along M/N; bits 46-48 = 0b001 (sm_100 family)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFF) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFF) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor, kind::f16: D f32, A and B bf16, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+// 32 lanes x 32 columns of 32-bit TMEM words: thread t of the warp gets lane
+// (lane base + t), columns col .. col + 31
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+        "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+        "=r"(v[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// ---- splitting -------------------------------------------------------------
+// biased FP64 exponent field of x (0 for zero and denormals)
+__device__ __forceinline__ int exp_field(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+// scale exponent of a row whose largest exponent field is ex: |x| < 2^e
+__device__ __forceinline__ int scale_of(int ex_max) { return ex_max - 1022; }
+
+// x 2^(55-e) rounded to an integer (|X| <= 2^55), split into kSlices balanced
+// base-256 digits, most significant first; integer operations only
+__device__ __forceinline__ void split7(double x, int e, int (&d)[kSlices]) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  long long X = 0;
+  if (ex != 0) {
+    const long long m = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+    const int sh = 1020 + e - ex;  // X = m 2^-sh, sh >= -2
+    if (sh <= 0)
+      X = m << (-sh);
+    else if (sh < 62)
+      X = (m + (1LL << (sh - 1))) >> sh;
+    if (bits < 0) X = -X;
+  }
+#pragma unroll
+  for (int s = 0; s < kSlices - 1; ++s) {
+    const int w = 8 * (kSlices - 1 - s);
+    const long long q = (X + (1LL << (w - 1))) >> w;
+    d[s] = (int)q;
+    X -= q << w;
+  }
+  d[kSlices - 1] = (int)X;
+}
+
+__device__ __forceinline__ uint32_t bf16_pair(int lo, int hi) {
+  return (__float_as_uint((float)lo) >> 16) | (__float_as_uint((float)hi) & 0xFFFF0000u);
+}
+
+// element offset of (row block rb, K chunk kc, slice s) + position (rr, kk) in it
+__device__ __forceinline__ long long plane_off(int s, long long kc, long long rb, long long nkc,
+                                               long long nrb, int rr, int kk) {
+  return ((s * nkc + kc) * nrb + rb) * 2048 + (rr >> 3) * 256 + (kk >> 3) * 64 + (rr & 7) * 8 +
+         (kk & 7);
+}
+
+// eight consecutive K values of one row -> kSlices 16-byte stores
+__device__ __forceinline__ void store_digits8(const double (&x)[8], int e, uint16_t* planes,
+                                              long long kc, long long rb, long long nkc,
+                                              long long nrb, int rr, int k0) {
+  int d[8][kSlices];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) split7(x[i], e, d[i]);
+#pragma unroll
+  for (int s = 0; s < kSlices; ++s) {
+    uint4 v;
+    v.x = bf16_pair(d[0][s], d[1][s]);
+    v.y = bf16_pair(d[2][s], d[3][s]);
+    v.z = bf16_pair(d[4][s], d[5][s]);
+    v.w = bf16_pair(d[6][s], d[7][s]);
+    *reinterpret_cast<uint4*>(planes + plane_off(s, kc, rb, nkc, nrb, rr, k0)) = v;
+  }
+}
+
+// one block per (padded) row: the largest exponent field of the row
+__global__ void k_row_expo(const double* __restrict__ X, long long rows, long long k,
+                           long long ld, int* __restrict__ expo) {
+  const long long r = blockIdx.x;
+  int mx = 0;
+  if (r < rows)
+    for (long long g = threadIdx.x; g < k; g += blockDim.x) mx = max(mx, exp_field(X[r * ld + g]));
+  __shared__ int red[32];
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    mx = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (threadIdx.x == 0) expo[r] = (r < rows) ? scale_of(mx) : 0;
+  }
+}
+
+// one block of 256 threads per (K chunk, row block): 64 rows x 32 K
+__global__ void __launch_bounds__(256) k_slice_rows(const double* __restrict__ X, long long rows,
+                                                    long long k, long long ld,
+                                                    const int* __restrict__ expo,
+                                                    uint16_t* __restrict__ planes, long long nkc,
+                                                    long long nrb) {
+  const long long kc = blockIdx.x, rb = blockIdx.y;
+  const int rr = threadIdx.x >> 2, k0 = (threadIdx.x & 3) * 8;
+  const long long row = rb * kBlockRows + rr;
+  const long long g0 = kc * kChunkK + k0;
+  double x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    x[i] = (row < rows && g0 + i < k) ? X[row * ld + g0 + i] : 0.0;
+  store_digits8(x, expo[row], planes, kc, rb, nkc, nrb, rr, k0);
+}
+
+// one thread per (padded) column g of X (kk x cols): exponent over the kk rows
+__global__ void k_col_expo(const double* __restrict__ X, long long kk, long long cols,
+                           long long ld, long long padded, int* __restrict__ expo) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < padded;
+       g += (long long)gridDim.x * blockDim.x) {
+    int mx = 0;
+    if (g < cols)
+      for (long long j = 0; j < kk; ++j) mx = max(mx, exp_field(X[j * ld + g]));
+    expo[g] = (g < cols) ? scale_of(mx) : 0;
+  }
+}
+
+// one block per (K chunk, row block) of the transpose: X rows j are the K
+// index, X columns g the operand rows; staged through shared memory
+__global__ void __launch_bounds__(256) k_slice_cols(const double* __restrict__ X, long long kk,
+                                                    long long cols, long long ld,
+                                                    const int* __restrict__ expo,
+                                                    uint16_t* __restrict__ planes, long long nkc,
+                                                    long long nrb) {
+  __shared__ double tile[kChunkK][kBlockRows + 1];
+  const long long kc = blockIdx.x, rb = blockIdx.y;
+  for (int e = threadIdx.x; e < kChunkK * kBlockRows; e += blockDim.x) {
+    const int j = e / kBlockRows, g = e % kBlockRows;
+    const long long jj = kc * kChunkK + j, gg = rb * kBlockRows + g;
+    tile[j][g] = (jj < kk && gg < cols) ? X[jj * ld + gg] : 0.0;
+  }
+  __syncthreads();
+  const int rr = threadIdx.x >> 2, k0 = (threadIdx.x & 3) * 8;
+  double x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = tile[k0 + i][rr];
+  store_digits8(x, expo[rb * kBlockRows + rr], planes, kc, rb, nkc, nrb, rr, k0);
+}
+
+// ---- the tensor-core contraction -------------------------------------------
+struct MmaArgs {
+  const uint16_t* A;
+  long long a_nrb;
+  const uint16_t* B;
+  long long b_nrb;
+  long long nkc;
+  const int* ea;
+  const int* eb;
+  int tiles_m, tiles_n, sym, ntiles, nsplit;
+  long long kc_per_split;
+  long long* part;  // nsplit > 1: part[hi/lo][split][prow][pcol]
+  long long prow, pcol;
+  double* C;  // nsplit == 1: direct
+  long long ldc, m, n;
+  double alpha;
+  int acc;  // add into C instead of overwriting it
+  int* err;
+};
+
+// v 2^k without overflow of the intermediate power (k = ea + eb - 38)
+__device__ __forceinline__ double pow2i(int k) {
+  return (k < -1022) ? 0.0 : __longlong_as_double((long long)(k + 1023) << 52);
+}
+__device__ __forceinline__ double scale2(double v, int k) {
+  const int k1 = k / 2;
+  return v * pow2i(k1) * pow2i(k - k1);
+}
+
+__device__ __forceinline__ void tile_of(const MmaArgs& a, int t, int& tm, int& tn) {
+  if (!a.sym) {
+    tm = t / a.tiles_n;
+    tn = t - tm * a.tiles_n;
+    return;
+  }
+  // tiles with a column >= a row: tn >= 2 tm
+  for (tm = 0; tm < a.tiles_m; ++tm) {
+    const int first = 2 * tm;
+    const int cnt = a.tiles_n > first ? a.tiles_n - first : 0;
+    if (t < cnt) {
+      tn = first + t;
+      return;
+    }
+    t -= cnt;
+  }
+  tm = tn = 0;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
+  extern __shared__ __align__(1024) uint8_t stage_mem[];
+  __shared__ __align__(8) uint64_t bar_load[kStages];
+  __shared__ __align__(8) uint64_t bar_mma;
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t smem0 = smem_u32(stage_mem);
+
+  if (tid == 0) {
+    for (int b = 0; b < kStages; ++b) mbar_init(smem_u32(&bar_load[b]), 1);
+    mbar_init(smem_u32(&bar_mma), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+  const int half = warp >> 2;  // which 32 of the tile's 64 columns this warp drains
+  constexpr uint32_t idesc = idesc_bf16(kTileM, kTileN);
+
+  uint32_t ph_load[kStages] = {0, 0};
+  uint32_t ph_mma = 0;
+  bool pending[kStages] = {false, false};
+  bool ok = true;
+  const int items = a.ntiles * a.nsplit;
+
+  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+    const int tile = item / a.nsplit, split = item - tile * a.nsplit;
+    int tm, tn;
+    tile_of(a, tile, tm, tn);
+    const long long kc0 = split * a.kc_per_split;
+    long long kc1 = kc0 + a.kc_per_split;
+    if (kc1 > a.nkc) kc1 = a.nkc;
+    const int nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);
+
+    long long Rh[32], Rl[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) Rh[c] = Rl[c] = 0;
+
+    auto issue = [&](long long kc, int buf) {
+      const uint32_t base = smem0 + buf * kStageBytes;
+      const uint32_t bar = smem_u32(&bar_load[buf]);
+      mbar_expect_tx(bar, kStageBytes);
+#pragma unroll 1
+      for (int s = 0; s < kSlices; ++s) {
+        const uint16_t* sa = a.A + ((s * a.nkc + kc) * a.a_nrb + 2LL * tm) * 2048;
+        const uint16_t* sb = a.B + ((s * a.nkc + kc) * a.b_nrb + tn) * 2048;
+        bulk_g2s(base + s * kSliceA, sa, kSliceA, bar);
+        bulk_g2s(base + kSlices * kSliceA + s * kSliceB, sb, kSliceB, bar);
+      }
+    };
+
+    if (nst > 0 && tid == 0) issue(kc0, 0);
+    pending[0] = nst > 0;
+    for (int st = 0; st < nst && ok; ++st) {
+      const int buf = st & 1;
+      if (st + 1 < nst) {
+        if (tid == 0) issue(kc0 + st + 1, buf ^ 1);
+        pending[buf ^ 1] = true;
+      }
+      ok = mbar_wait(smem_u32(&bar_load[buf]), ph_load[buf], a.err, 1);
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      ph_load[buf] ^= 1;
+      pending[buf] = false;
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t base = smem0 + buf * kStageBytes;
+        const bool fresh = (st % kStagesPerDrain) == 0;
+#pragma unroll 1
+        for (int s = 0; s < kSlices; ++s) {
+#pragma unroll 1
+          for (int t = 0; t < kSlices - s; ++t) {
+            const uint32_t d = tmem + (uint32_t)((s + t) * kTileN);
+#pragma unroll
+            for (int ks = 0; ks < kChunkK / 16; ++ks) {
+              const uint64_t da = smem_desc(base + s * kSliceA + ks * 256, 128, 512);
+              const uint64_t db = smem_desc(base + kSlices * kSliceA + t * kSliceB + ks * 256,
+                                            128, 512);
+              mma_bf16(d, da, db, idesc, (fresh && s == 0 && ks == 0) ? 0u : 1u);
+            }
+          }
+        }
+        mma_commit(smem_u32(&bar_mma));
+      }
+      ok = mbar_wait(smem_u32(&bar_mma), ph_mma, a.err, 2);
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      ph_mma ^= 1;
+      if ((st % kStagesPerDrain) == kStagesPerDrain - 1 || st == nst - 1) {
+        tc_fence_after();
+#pragma unroll
+        for (int l = 0; l < kSlices; ++l) {
+          uint32_t v[32];
+          tmem_ld32(tmem + lane_base + (uint32_t)(l * kTileN + half * 32), v);
+#pragma unroll
+          for (int c = 0; c < 32; ++c) {
+            const long long w = (long long)__float2int_rn(__uint_as_float(v[c]));
+            if (l <= 3)
+              Rh[c] += w << (24 - 8 * l);
+            else
+              Rl[c] += w << (48 - 8 * l);
+          }
+        }
+        tc_fence_before();
+        __syncthreads();
+      }
+    }
+    if (!ok) break;
+    // output row 32 (warp % 4) + lane, columns 32 half .. + 31 of tile (tm, tn)
+    const long long i = (long long)tm * kTileM + (warp & 3) * 32 + (tid & 31);
+    const long long j0 = (long long)tn * kTileN + half * 32;
+    if (a.nsplit > 1) {
+      long long* dh = a.part + ((long long)split * a.prow + i) * a.pcol + j0;
+      long long* dl = dh + (long long)a.nsplit * a.prow * a.pcol;
+#pragma unroll
+      for (int c = 0; c < 32; c += 2) {
+        *reinterpret_cast<longlong2*>(dh + c) = make_longlong2(Rh[c], Rh[c + 1]);
+        *reinterpret_cast<longlong2*>(dl + c) = make_longlong2(Rl[c], Rl[c + 1]);
+      }
+    } else if (i < a.m) {
+      const int ei = a.ea[i];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const long long j = j0 + c;
+        if (j < a.n && (!a.sym || j >= i)) {
+          const double r = (double)Rh[c] + (double)Rl[c] * 0x1p-24;
+          const double v = scale2(a.alpha * r, ei + a.eb[j] - 38);
+          a.C[i * a.ldc + j] = a.acc ? a.C[i * a.ldc + j] + v : v;
+          if (a.sym && j > i) a.C[j * a.ldc + i] = a.acc ? a.C[j * a.ldc + i] + v : v;
+        }
+      }
+    }
+  }
+  if (!ok && tid == 0) {
+    // let copies still in flight land before the shared memory is released
+    for (int b = 0; b < kStages; ++b)
+      if (pending[b]) mbar_wait(smem_u32(&bar_load[b]), ph_load[b], a.err, 3);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemCols)
+                 : "memory");
+}
+
+// C = alpha 2^(ea + eb - 38) (hi + lo 2^-24), hi and lo the integer sums of
+// the split-K partials
+__global__ void k_oz_reduce(const long long* __restrict__ part, int nsplit, long long prow,
+                            long long pcol, const int* __restrict__ ea,
+                            const int* __restrict__ eb, long long m, long long n, double alpha,
+                            int sym, int acc, double* __restrict__ C, long long ldc) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < m * n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long i = idx / n, j = idx - i * n;
+    long long ii = i, jj = j;
+    if (sym && j < i) {
+      ii = j;
+      jj = i;
+    }
+    long long sh = 0, sl = 0;
+    const long long lo = (long long)nsplit * prow * pcol;
+    for (int sp = 0; sp < nsplit; ++sp) {
+      const long long o = ((long long)sp * prow + ii) * pcol + jj;
+      sh += part[o];
+      sl += part[lo + o];
+    }
+    const double v = scale2(alpha * ((double)sh + (double)sl * 0x1p-24), ea[ii] + eb[jj] - 38);
+    C[i * ldc + j] = acc ? C[i * ldc + j] + v : v;
+  }
+}
+
+}  // namespace
+}  // namespace oz
+}  // namespace sep
+
+// ---- host side ---------------------------------------------------------------
+namespace sep {
+namespace oz {
+
+namespace {
+long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
+long long padded_blocks(long long rows) { return 2 * cdiv(rows, kTileM); }  // 64-row blocks
+int sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+int tile_count(long long m, long long n, bool sym) {
+  const int tmc = (int)cdiv(m, kTileM), tnc = (int)cdiv(n, kTileN);
+  if (!sym) return tmc * tnc;
+  int t = 0;
+  for (int tm = 0; tm < tmc; ++tm) t += tnc > 2 * tm ? tnc - 2 * tm : 0;
+  return t;
+}
+}  // namespace
+
+size_t plane_elems(long long rows, long long k) {
+  return (size_t)kSlices * (size_t)cdiv(k, kChunkK) * (size_t)padded_blocks(rows) * 2048;
+}
+
+cudaError_t slice_rows(const double* X, long long rows, long long k, long long ld, Planes& p,
+                       cudaStream_t s) {
+  p.rows = rows;
+  p.k = k;
+  p.nrb = padded_blocks(rows);
+  p.nkc = cdiv(k, kChunkK);
+  if (p.nkc > 0x7fffffffLL || p.nrb > 65535) return cudaErrorInvalidValue;
+  k_row_expo<<<(unsigned)(p.nrb * kBlockRows), 256, 0, s>>>(X, rows, k, ld, p.expo);
+  k_slice_rows<<<dim3((unsigned)p.nkc, (unsigned)p.nrb), 256, 0, s>>>(X, rows, k, ld, p.expo,
+                                                                      p.d, p.nkc, p.nrb);
+  return cudaGetLastError();
+}
+
+cudaError_t slice_cols(const double* X, long long kk, long long cols, long long ld, Planes& p,
+                       cudaStream_t s) {
+  p.rows = cols;
+  p.k = kk;
+  p.nrb = padded_blocks(cols);
+  p.nkc = cdiv(kk, kChunkK);
+  if (p.nkc > 0x7fffffffLL || p.nrb > 65535) return cudaErrorInvalidValue;
+  const long long padded = p.nrb * kBlockRows;
+  k_col_expo<<<(unsigned)std::min<long long>(cdiv(padded, 256), 152LL * 16), 256, 0, s>>>(
+      X, kk, cols, ld, padded, p.expo);
+  k_slice_cols<<<dim3((unsigned)p.nkc, (unsigned)p.nrb), 256, 0, s>>>(X, kk, cols, ld, p.expo,
+                                                                      p.d, p.nkc, p.nrb);
+  return cudaGetLastError();
+}
+
+size_t part_elems(long long m, long long n, int nsplit) {
+  if (nsplit <= 1) return 0;
+  return 2 * (size_t)nsplit * (size_t)(cdiv(m, kTileM) * kTileM) *
+         (size_t)(cdiv(n, kTileN) * kTileN);
+}
+
+int choose_splits(long long m, long long n, long long k, bool sym) {
+  const long long tiles = tile_count(m, n, sym);
+  const long long nkc = cdiv(k, kChunkK);
+  long long ns = cdiv(sm_count(), tiles);
+  const long long cap = std::max<long long>(1, nkc / (2 * (kDrainK / kChunkK)));
+  if (ns > cap) ns = cap;
+  if (ns < 1) ns = 1;
+  return (int)ns;
+}
+
+cudaError_t gemm_nt(const Planes& A, const Planes& B, double alpha, bool sym, bool accumulate,
+                    double* C, long long ldc, long long* part, int nsplit, int* err,
+                    cudaStream_t s) {
+  if (A.nkc != B.nkc || A.k != B.k) return cudaErrorInvalidValue;
+  if (nsplit > 1 && !part) return cudaErrorInvalidValue;
+  static bool attr_set[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    e = cudaFuncSetAttribute(k_oz_mma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kStages * kStageBytes);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = true;
+  }
+  MmaArgs a{};
+  a.A = A.d;
+  a.a_nrb = A.nrb;
+  a.B = B.d;
+  a.b_nrb = B.nrb;
+  a.nkc = A.nkc;
+  a.ea = A.expo;
+  a.eb = B.expo;
+  a.m = A.rows;
+  a.n = B.rows;
+  a.tiles_m = (int)cdiv(A.rows, kTileM);
+  a.tiles_n = (int)cdiv(B.rows, kTileN);
+  a.sym = sym ? 1 : 0;
+  a.ntiles = tile_count(A.rows, B.rows, sym);
+  a.nsplit = nsplit < 1 ? 1 : nsplit;
+  a.kc_per_split = cdiv(A.nkc, a.nsplit);
+  a.part = part;
+  a.prow = (long long)a.tiles_m * kTileM;
+  a.pcol = (long long)a.tiles_n * kTileN;
+  a.C = C;
+  a.ldc = ldc;
+  a.alpha = alpha;
+  a.acc = accumulate ? 1 : 0;
+  a.err = err;
+  const long long items = (long long)a.ntiles * a.nsplit;
+  if (items < 1) return cudaSuccess;
+  const unsigned grid = (unsigned)std::min<long long>(items, sm_count());
+  k_oz_mma<<<grid, kThreads, kStages * kStageBytes, s>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || a.nsplit == 1) return e;
+  const long long mn = A.rows * B.rows;
+  k_oz_reduce<<<(unsigned)std::min<long long>(cdiv(mn, 256), 152LL * 8), 256, 0, s>>>(
+      part, a.nsplit, a.prow, a.pcol, A.expo, B.expo, A.rows, B.rows, alpha, a.sym, a.acc, C, ldc);
+  return cudaGetLastError();
+}
+
+cudaError_t check_status(const int* err, cudaStream_t s, int* host_status) {
+  cudaError_t e = cudaMemcpyAsync(host_status, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
+}  // namespace oz
+}  // namespace sep

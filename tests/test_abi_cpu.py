@@ -91,33 +91,25 @@ def test_bad_arguments_raise():
         sep.start_states(-1, 0, 10, 1.0)
 
 
-def test_form_factor_jacobian_matches_central_differences():
-    from semi_empirical_pseudopotentials_gb300 import adjoint
-
+def test_form_factor_backward_matches_central_differences():
+    """sep_form_factor_backward (shift adjoint + sine-transform Jacobian) against
+    central differences of w . shifted_table(a), all on the host."""
     a = np.array([10.2, 1.45, 29.0, 0.31])
     vol = 189.6
-    r, v, jac = adjoint.form_factor_jacobian(a, vol)
+    w = np.random.default_rng(0).standard_normal(1024)
+
+    def L(p):
+        v = sep.form_factor_table(p, vol)[1]
+        return float(w @ (v - v[-1]))
+
+    g = sep.form_factor_backward(a, vol, w)
     for j in range(4):
         h = 1e-6 * max(1.0, abs(a[j]))
         ap, am = a.copy(), a.copy()
         ap[j] += h
         am[j] -= h
-        fd = (sep.form_factor_table(ap, vol)[1] - sep.form_factor_table(am, vol)[1]) / (2 * h)
-        assert np.abs(fd - jac[j]).max() <= 1e-6 * np.abs(jac[j]).max() + 1e-12
-
-
-def test_shift_backward_is_the_adjoint():
-    from semi_empirical_pseudopotentials_gb300 import adjoint
-
-    rng = np.random.default_rng(0)
-    raw, d = rng.standard_normal(50), rng.standard_normal(50)
-    w = rng.standard_normal(50)
-
-    def shifted(x):
-        return x - x[-1]
-
-    lin = w @ (shifted(raw + 1e-3 * d) - shifted(raw)) / 1e-3
-    assert abs(lin - adjoint.shift_backward(w, 50) @ d) < 1e-9
+        fd = (L(ap) - L(am)) / (2 * h)
+        assert abs(fd - g[j]) <= 1e-6 * np.abs(g).max(), (j, fd, g[j])
 
 
 def test_band_edge_selection():
