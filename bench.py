@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark of the filter-diagonalisation path on one GB300 (or N replicas).
 
-Workload (BASELINE config 1): zincblende CdSe-like sphere of radius 2.5 nm
+Workload: zincblende CdSe-like sphere of radius 2.5 nm
 (2317 atoms, seeded form factors), 128^3 grid, 64 start states x 8 target
 energies, Newton filter length 1024, the filter's H psi chain in complex64
 with FP32 accumulation.  Synthetic inputs (no dataset is involved).
@@ -49,12 +49,13 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="skip FP64 sample, pipeline, roofline and CPU baseline")
     p.add_argument("--batched", action="store_true",
-                   help="BASELINE config 3: 32 uneven nanocrystals in one graph launch vs "
+                   help="32 uneven nanocrystals (48^3 .. 112^3) in one graph launch vs "
                         "32 sequential launches")
-    p.add_argument("--profile", choices=["mixed", "f64"], default=None,
-                   help="run only a small filter case for an ncu capture: 24 (mixed) or 16 "
+    p.add_argument("--profile", choices=["mixed", "f64", "subspace"], default=None,
+                   help="run only a small case for an ncu capture: 24 (mixed) or 16 "
                         "(f64) start states x 8 Newton steps of the 128^3 workload (3.5 GB "
-                        "and 4.8 GB on the device)")
+                        "and 4.8 GB on the device), or (subspace) the tensor-core Gram of "
+                        "512 states x 262144 points (1.1 GB)")
     return p.parse_args()
 
 
@@ -64,6 +65,14 @@ def run_profile(args):
 
     S = build_system()
     tr, tv = tables(sep, S)
+    if args.profile == "subspace":
+        ctx = sep.Context((64, 64, 64), (1.0, 1.0, 1.0), potl=np.zeros(64 ** 3))
+        A = np.random.default_rng(3).standard_normal((512, 1 << 18))
+        for _ in range(2):
+            G = ctx.subspace_gemm(A)
+        print(json.dumps({"profile_case": "subspace", "m": 512, "k": 1 << 18,
+                          "checksum": float(np.trace(G))}))
+        return
     ctx = sep.Context(S.dims, S.steps, precision=args.profile)
     ctx.set_block_steps(8)
     ctx.set_graphs(False)
@@ -97,6 +106,57 @@ def tables(sep, S):
         r, v = sep.form_factor_table(S.params[t], S.vol_per_atom)
         tr[t], tv[t] = r, v - v[-1]
     return tr, tv
+
+
+def warm_pipeline(sep):
+    """One small pipeline (32^3 Gaussian well, 8 states) to load the kernels of
+    the eigensolver and of the subspace contractions before timed runs."""
+    n = 32
+    x = (np.arange(n) - n / 2) * 0.8
+    r2 = x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2
+    pot = (-2.0 * np.exp(-r2 / 20.0)).ravel()
+    c = sep.Context((n, n, n), (0.8, 0.8, 0.8), potl=pot, precision="mixed")
+    start = sep.start_states(-5, 4, n ** 3, 0.8 ** 3)
+    c.pipeline(start, [-1.5, -1.0], 64, float(pot.min()))
+    c.close()
+
+
+def subspace_gram(sep, ctx, psi_d, m, n, dv, peaks):
+    """Gram matrix of the m filtered states (the first contraction of ortho,
+    filter/ortho.c:11-52) on the tensor cores and on the FP64 pipe, device
+    resident, CUDA events on the library's stream."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    G = torch.empty((m, m), dtype=torch.float64, device=psi_d.device)
+    res = {"shape": f"{m} states x {n} points", "kernel": "k_oz_mma (+ slicing, split-K sum)"}
+    times = {}
+    for mode in ("tc", "f64"):
+        ctx.set_subspace(mode)
+        ctx.subspace_gemm_dev(psi_d.data_ptr(), psi_d.data_ptr(), m, m, n, G.data_ptr(), dv, True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.subspace_gemm_dev(psi_d.data_ptr(), psi_d.data_ptr(), m, m, n, G.data_ptr(), dv, True)
+        e1.record(stream)
+        e1.synchronize()
+        times[mode] = e0.elapsed_time(e1) * 1e-3
+        if mode == "tc":
+            g_tc = G.clone()
+    ctx.set_subspace("tc")
+    # 20 output tiles of 128 x 64 cover the upper triangle of 512 x 512; each
+    # tile runs 28 bf16 products of 128 x 64 x n
+    tiles = sum(max(0, -(-m // 64) - 2 * t) for t in range(-(-m // 128)))
+    bf16_flops = 28 * 2.0 * 128 * 64 * n * tiles
+    res.update({
+        "tc_ms": round(1e3 * times["tc"], 3), "fp64_pipe_ms": round(1e3 * times["f64"], 3),
+        "speedup": times["f64"] / times["tc"],
+        "fp64_equivalent_tflops": m * (m + 1) * n / times["tc"] / 1e12,
+        "tensor_bf16_tflops": bf16_flops / times["tc"] / 1e12,
+        "tensor_frac_of_measured_bf16": bf16_flops / times["tc"] / 1e12 / peaks["bf16_tflops"],
+        "max_abs_diff_tc_vs_f64_pipe": float((g_tc - G).abs().max().item()),
+        "max_abs_entry": float(G.abs().max().item())})
+    return res
 
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum per pair, 128^3 complex64,
@@ -411,11 +471,16 @@ def run_sep(args):
                           "per_launch_ms": dict(zip(names, [round(p, 4) for p in per64])),
                           "note": "complex128 line passes run at the FP64 pipe rate "
                                   "(about 1.25 TFLOP/s on this part)"}
+        extras["subspace_gram"] = subspace_gram(sep, ctx, out_d, ns * ms, n, S.dv, peaks)
         # whole path: energy range -> filter -> ortho -> Rayleigh-Ritz -> sigma,
         # mixed and plain FP64 on the same start states
         del out_d
         torch.cuda.empty_cache()
-        ttb = {"window": [float(S.el[0]), float(S.el[-1])]}
+        ttb = {"window": [float(S.el[0]), float(S.el[-1])],
+               "note": "warm calls: a small pipeline runs first, so the one-time loading of "
+                       "the eigensolver's and the contraction kernels (about 3 s per "
+                       "process) is not in the timed runs"}
+        warm_pipeline(sep)
         conv, inwin_vals = {}, {}
         for tag, cx_ in (("mixed", ctx), ("f64", ctx64)):
             res = cx_.pipeline(start_h, S.el, nc, vmin)

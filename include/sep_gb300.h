@@ -240,6 +240,10 @@ int sep_ctx_set_subspace(sep_ctx *ctx, int mode);
  * (B may be NULL) and C is symmetric.  Uses the context's mode. */
 int sep_subspace_gemm(sep_ctx *ctx, const double *A, const double *B, long m, long n, long k,
                       double alpha, int sym, double *C);
+/* The same on device pointers, on the context's stream; in mode 1 it waits
+ * for the stream before returning (it reads the kernel's status word). */
+int sep_subspace_gemm_dev(sep_ctx *ctx, const double *A, const double *B, long m, long n,
+                          long k, double alpha, int sym, double *C);
 /* out (m x w) = W (m x k) X (k x w), host row-major.  Uses the context's mode. */
 int sep_subspace_rotate(sep_ctx *ctx, const double *W, const double *X, long m, long k, long w,
                         double *out);

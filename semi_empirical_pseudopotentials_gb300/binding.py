@@ -96,6 +96,8 @@ def lib():
         L.sep_subspace_gemm.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, C.c_double,
                                         C.c_int, dp]
         L.sep_subspace_rotate.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, dp]
+        L.sep_subspace_gemm_dev.argtypes = [vp, vp, vp, C.c_long, C.c_long, C.c_long, C.c_double,
+                                            C.c_int, vp]
         L.sep_potential_from_params.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, C.c_double,
                                                 dp, dp]
         L.sep_band_edge_backward.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, C.c_double,
@@ -366,6 +368,11 @@ class Context:
         _check(lib().sep_subspace_gemm(self.h, _p(A), None if sym else _p(Bm), A.shape[0],
                                        Bm.shape[0], A.shape[1], alpha, 1 if sym else 0, _p(out)))
         return out
+
+    def subspace_gemm_dev(self, A_ptr, B_ptr, m, n, k, C_ptr, alpha=1.0, sym=False):
+        """Device-pointer form on the context's stream."""
+        _check(lib().sep_subspace_gemm_dev(self.h, A_ptr, B_ptr, m, n, k, alpha, 1 if sym else 0,
+                                           C_ptr))
 
     def subspace_rotate(self, W, X):
         """W X through the context's subspace contraction."""

@@ -633,6 +633,14 @@ int sep_subspace_gemm(sep_ctx* c, const double* A, const double* B, long m, long
   return kOk;
 }
 
+int sep_subspace_gemm_dev(sep_ctx* c, const double* A, const double* B, long m, long n, long k,
+                          double alpha, int sym, double* C) {
+  RET(check_ctx(c, false));
+  if (!A || !C || (!sym && !B) || m < 1 || n < 1 || k < 1 || (sym && m != n))
+    return arg_fail("sep_subspace_gemm_dev: bad argument");
+  return subspace_gemm_device(c, A, sym ? A : B, m, n, k, alpha, sym != 0, C);
+}
+
 int sep_subspace_rotate(sep_ctx* c, const double* W, const double* X, long m, long k, long w,
                         double* out) {
   RET(check_ctx(c, false));

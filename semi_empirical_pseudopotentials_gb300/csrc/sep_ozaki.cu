@@ -22,12 +22,12 @@ namespace oz {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kStages = 2;
-constexpr int kSliceA = kTileM * kChunkK * 2;               // 8192 bytes
-constexpr int kSliceB = kTileN * kChunkK * 2;               // 4096 bytes
-constexpr int kStageBytes = kSlices * (kSliceA + kSliceB);  // 86016 bytes
+constexpr int kStages = 4;
+constexpr int kSliceA = kTileM * kChunkK * 2;               // 4096 bytes
+constexpr int kSliceB = kTileN * kChunkK * 2;               // 2048 bytes
+constexpr int kStageBytes = kSlices * (kSliceA + kSliceB);  // 43008 bytes
 constexpr int kTmemCols = 512;                              // kSlices * 64 = 448 used
-constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 4
+constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 8
 constexpr long long kSpin = 1LL << 26;                      // bounded waits
 static_assert(kSlices * kTileN <= kTmemCols, "TMEM columns");
 static_assert((kSlices) * kDrainK * 16384LL < (1LL << 24), "exact FP32 level sums");
@@ -175,8 +175,8 @@ __device__ __forceinline__ uint32_t bf16_pair(int lo, int hi) {
 // element offset of (row block rb, K chunk kc, slice s) + position (rr, kk) in it
 __device__ __forceinline__ long long plane_off(int s, long long kc, long long rb, long long nkc,
                                                long long nrb, int rr, int kk) {
-  return ((s * nkc + kc) * nrb + rb) * 2048 + (rr >> 3) * 256 + (kk >> 3) * 64 + (rr & 7) * 8 +
-         (kk & 7);
+  return ((s * nkc + kc) * nrb + rb) * kBlockElems + (rr >> 3) * (kChunkK * 8) + (kk >> 3) * 64 +
+         (rr & 7) * 8 + (kk & 7);
 }
 
 // eight consecutive K values of one row -> kSlices 16-byte stores
@@ -215,14 +215,16 @@ __global__ void k_row_expo(const double* __restrict__ X, long long rows, long lo
   }
 }
 
-// one block of 256 threads per (K chunk, row block): 64 rows x 32 K
-__global__ void __launch_bounds__(256) k_slice_rows(const double* __restrict__ X, long long rows,
+// one block per (K chunk, row block): 64 rows x kChunkK values of K, eight
+// consecutive K values per thread
+constexpr int kSliceThreads = kBlockRows * kChunkK / 8;
+__global__ void __launch_bounds__(kSliceThreads) k_slice_rows(const double* __restrict__ X, long long rows,
                                                     long long k, long long ld,
                                                     const int* __restrict__ expo,
                                                     uint16_t* __restrict__ planes, long long nkc,
                                                     long long nrb) {
   const long long kc = blockIdx.x, rb = blockIdx.y;
-  const int rr = threadIdx.x >> 2, k0 = (threadIdx.x & 3) * 8;
+  const int rr = threadIdx.x / (kChunkK / 8), k0 = (threadIdx.x % (kChunkK / 8)) * 8;
   const long long row = rb * kBlockRows + rr;
   const long long g0 = kc * kChunkK + k0;
   double x[8];
@@ -246,7 +248,7 @@ __global__ void k_col_expo(const double* __restrict__ X, long long kk, long long
 
 // one block per (K chunk, row block) of the transpose: X rows j are the K
 // index, X columns g the operand rows; staged through shared memory
-__global__ void __launch_bounds__(256) k_slice_cols(const double* __restrict__ X, long long kk,
+__global__ void __launch_bounds__(kSliceThreads) k_slice_cols(const double* __restrict__ X, long long kk,
                                                     long long cols, long long ld,
                                                     const int* __restrict__ expo,
                                                     uint16_t* __restrict__ planes, long long nkc,
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(256) k_slice_cols(const double* __restrict__ X
     tile[j][g] = (jj < kk && gg < cols) ? X[jj * ld + gg] : 0.0;
   }
   __syncthreads();
-  const int rr = threadIdx.x >> 2, k0 = (threadIdx.x & 3) * 8;
+  const int rr = threadIdx.x / (kChunkK / 8), k0 = (threadIdx.x % (kChunkK / 8)) * 8;
   double x[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) x[i] = tile[k0 + i][rr];
@@ -317,14 +319,18 @@ __device__ __forceinline__ void tile_of(const MmaArgs& a, int t, int& tm, int& t
 __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
   extern __shared__ __align__(1024) uint8_t stage_mem[];
   __shared__ __align__(8) uint64_t bar_load[kStages];
-  __shared__ __align__(8) uint64_t bar_mma;
+  __shared__ __align__(8) uint64_t bar_free[kStages];
+  __shared__ __align__(8) uint64_t bar_drain;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t smem0 = smem_u32(stage_mem);
 
   if (tid == 0) {
-    for (int b = 0; b < kStages; ++b) mbar_init(smem_u32(&bar_load[b]), 1);
-    mbar_init(smem_u32(&bar_mma), 1);
+    for (int b = 0; b < kStages; ++b) {
+      mbar_init(smem_u32(&bar_load[b]), 1);
+      mbar_init(smem_u32(&bar_free[b]), 1);
+    }
+    mbar_init(smem_u32(&bar_drain), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -342,20 +348,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
   const int half = warp >> 2;  // which 32 of the tile's 64 columns this warp drains
   constexpr uint32_t idesc = idesc_bf16(kTileM, kTileN);
 
-  uint32_t ph_load[kStages] = {0, 0};
-  uint32_t ph_mma = 0;
-  bool pending[kStages] = {false, false};
+  // thread 0's bookkeeping: load phases consumed, commits issued per buffer
+  uint32_t ph_load[kStages], n_commit[kStages];
+  bool pending[kStages];
+  for (int b = 0; b < kStages; ++b) {
+    ph_load[b] = 0;
+    n_commit[b] = 0;
+    pending[b] = false;
+  }
+  uint32_t ph_drain = 0;
   bool ok = true;
   const int items = a.ntiles * a.nsplit;
+  long long gstage = 0;  // stages consumed by this CTA so far (buffer = gstage % kStages)
 
   for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
-    const int tile = item / a.nsplit, split = item - tile * a.nsplit;
+    // split-major order: CTAs running together share K ranges (and L2 lines)
+    const int split = item / a.ntiles, tile = item - split * a.ntiles;
     int tm, tn;
     tile_of(a, tile, tm, tn);
     const long long kc0 = split * a.kc_per_split;
     long long kc1 = kc0 + a.kc_per_split;
     if (kc1 > a.nkc) kc1 = a.nkc;
-    const int nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);
+    const int nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);  // the host leaves no split empty
 
     long long Rh[32], Rl[32];
 #pragma unroll
@@ -367,51 +381,59 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
       mbar_expect_tx(bar, kStageBytes);
 #pragma unroll 1
       for (int s = 0; s < kSlices; ++s) {
-        const uint16_t* sa = a.A + ((s * a.nkc + kc) * a.a_nrb + 2LL * tm) * 2048;
-        const uint16_t* sb = a.B + ((s * a.nkc + kc) * a.b_nrb + tn) * 2048;
+        const uint16_t* sa = a.A + ((s * a.nkc + kc) * a.a_nrb + 2LL * tm) * kBlockElems;
+        const uint16_t* sb = a.B + ((s * a.nkc + kc) * a.b_nrb + tn) * kBlockElems;
         bulk_g2s(base + s * kSliceA, sa, kSliceA, bar);
         bulk_g2s(base + kSlices * kSliceA + s * kSliceB, sb, kSliceB, bar);
       }
+      pending[buf] = true;
     };
 
-    if (nst > 0 && tid == 0) issue(kc0, 0);
-    pending[0] = nst > 0;
-    for (int st = 0; st < nst && ok; ++st) {
-      const int buf = st & 1;
-      if (st + 1 < nst) {
-        if (tid == 0) issue(kc0 + st + 1, buf ^ 1);
-        pending[buf ^ 1] = true;
-      }
-      ok = mbar_wait(smem_u32(&bar_load[buf]), ph_load[buf], a.err, 1);
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      ph_load[buf] ^= 1;
-      pending[buf] = false;
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t base = smem0 + buf * kStageBytes;
-        const bool fresh = (st % kStagesPerDrain) == 0;
+    // prologue: every buffer is free (the previous item ended with a drain,
+    // which waited for all of its tensor-core work)
+    if (tid == 0)
+      for (int j = 0; j < kStages && j < nst; ++j) issue(kc0 + j, (int)((gstage + j) % kStages));
+
+    for (int st = 0; st < nst; ++st) {
+      const int buf = (int)((gstage + st) % kStages);
+      const bool drain_now = (st % kStagesPerDrain) == kStagesPerDrain - 1 || st == nst - 1;
+      if (tid == 0 && ok) {
+        ok = mbar_wait(smem_u32(&bar_load[buf]), ph_load[buf], a.err, 1);
+        if (ok) {
+          ph_load[buf] ^= 1;
+          pending[buf] = false;
+          tc_fence_after();
+          const uint32_t base = smem0 + buf * kStageBytes;
+          const bool fresh = (st % kStagesPerDrain) == 0;
 #pragma unroll 1
-        for (int s = 0; s < kSlices; ++s) {
+          for (int s = 0; s < kSlices; ++s) {
+            const uint64_t da = smem_desc(base + s * kSliceA, 128, kChunkK * 16);
 #pragma unroll 1
-          for (int t = 0; t < kSlices - s; ++t) {
-            const uint32_t d = tmem + (uint32_t)((s + t) * kTileN);
-#pragma unroll
-            for (int ks = 0; ks < kChunkK / 16; ++ks) {
-              const uint64_t da = smem_desc(base + s * kSliceA + ks * 256, 128, 512);
-              const uint64_t db = smem_desc(base + kSlices * kSliceA + t * kSliceB + ks * 256,
-                                            128, 512);
-              mma_bf16(d, da, db, idesc, (fresh && s == 0 && ks == 0) ? 0u : 1u);
+            for (int t = 0; t < kSlices - s; ++t) {
+              const uint64_t db =
+                  smem_desc(base + kSlices * kSliceA + t * kSliceB, 128, kChunkK * 16);
+              mma_bf16(tmem + (uint32_t)((s + t) * kTileN), da, db, idesc,
+                       (fresh && s == 0) ? 0u : 1u);
             }
           }
+          mma_commit(smem_u32(&bar_free[buf]));
+          n_commit[buf]++;
+          if (drain_now) mma_commit(smem_u32(&bar_drain));
+          // refill the buffer of the previous stage once its products are done
+          if (st >= 1 && st - 1 + kStages < nst) {
+            const int pb = (int)((gstage + st - 1) % kStages);
+            ok = mbar_wait(smem_u32(&bar_free[pb]), (n_commit[pb] - 1) & 1, a.err, 2);
+            if (ok) issue(kc0 + st - 1 + kStages, pb);
+          }
         }
-        mma_commit(smem_u32(&bar_mma));
       }
-      ok = mbar_wait(smem_u32(&bar_mma), ph_mma, a.err, 2);
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      ph_mma ^= 1;
-      if ((st % kStagesPerDrain) == kStagesPerDrain - 1 || st == nst - 1) {
+      if (drain_now) {
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        ok = mbar_wait(smem_u32(&bar_drain), ph_drain, a.err, 3);
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        ph_drain ^= 1;
         tc_fence_after();
 #pragma unroll
         for (int l = 0; l < kSlices; ++l) {
@@ -430,6 +452,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
         __syncthreads();
       }
     }
+    gstage += nst;
+    if (!ok) break;
+    // consume the last commit of every buffer (all complete after the drain)
+    if (tid == 0)
+      for (int b = 0; b < kStages && ok; ++b)
+        if (n_commit[b] > 0) ok = mbar_wait(smem_u32(&bar_free[b]), (n_commit[b] - 1) & 1, a.err, 5);
+    ok = __syncthreads_and(ok);
     if (!ok) break;
     // output row 32 (warp % 4) + lane, columns 32 half .. + 31 of tile (tm, tn)
     const long long i = (long long)tm * kTileM + (warp & 3) * 32 + (tid & 31);
@@ -459,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
   if (!ok && tid == 0) {
     // let copies still in flight land before the shared memory is released
     for (int b = 0; b < kStages; ++b)
-      if (pending[b]) mbar_wait(smem_u32(&bar_load[b]), ph_load[b], a.err, 3);
+      if (pending[b]) mbar_wait(smem_u32(&bar_load[b]), ph_load[b], a.err, 4);
   }
   tc_fence_before();
   __syncthreads();
@@ -522,7 +551,7 @@ int tile_count(long long m, long long n, bool sym) {
 }  // namespace
 
 size_t plane_elems(long long rows, long long k) {
-  return (size_t)kSlices * (size_t)cdiv(k, kChunkK) * (size_t)padded_blocks(rows) * 2048;
+  return (size_t)kSlices * (size_t)cdiv(k, kChunkK) * (size_t)padded_blocks(rows) * kBlockElems;
 }
 
 cudaError_t slice_rows(const double* X, long long rows, long long k, long long ld, Planes& p,
@@ -533,7 +562,7 @@ cudaError_t slice_rows(const double* X, long long rows, long long k, long long l
   p.nkc = cdiv(k, kChunkK);
   if (p.nkc > 0x7fffffffLL || p.nrb > 65535) return cudaErrorInvalidValue;
   k_row_expo<<<(unsigned)(p.nrb * kBlockRows), 256, 0, s>>>(X, rows, k, ld, p.expo);
-  k_slice_rows<<<dim3((unsigned)p.nkc, (unsigned)p.nrb), 256, 0, s>>>(X, rows, k, ld, p.expo,
+  k_slice_rows<<<dim3((unsigned)p.nkc, (unsigned)p.nrb), kSliceThreads, 0, s>>>(X, rows, k, ld, p.expo,
                                                                       p.d, p.nkc, p.nrb);
   return cudaGetLastError();
 }
@@ -548,7 +577,7 @@ cudaError_t slice_cols(const double* X, long long kk, long long cols, long long 
   const long long padded = p.nrb * kBlockRows;
   k_col_expo<<<(unsigned)std::min<long long>(cdiv(padded, 256), 152LL * 16), 256, 0, s>>>(
       X, kk, cols, ld, padded, p.expo);
-  k_slice_cols<<<dim3((unsigned)p.nkc, (unsigned)p.nrb), 256, 0, s>>>(X, kk, cols, ld, p.expo,
+  k_slice_cols<<<dim3((unsigned)p.nkc, (unsigned)p.nrb), kSliceThreads, 0, s>>>(X, kk, cols, ld, p.expo,
                                                                       p.d, p.nkc, p.nrb);
   return cudaGetLastError();
 }
@@ -560,13 +589,26 @@ size_t part_elems(long long m, long long n, int nsplit) {
 }
 
 int choose_splits(long long m, long long n, long long k, bool sym) {
+  // enough items for every SM, and the item count close to a multiple of the
+  // SM count (items run in waves of one per SM); each split covers at least
+  // two drain periods of K
   const long long tiles = tile_count(m, n, sym);
   const long long nkc = cdiv(k, kChunkK);
-  long long ns = cdiv(sm_count(), tiles);
+  const long long sms = sm_count();
   const long long cap = std::max<long long>(1, nkc / (2 * (kDrainK / kChunkK)));
-  if (ns > cap) ns = cap;
-  if (ns < 1) ns = 1;
-  return (int)ns;
+  long long best = 1;
+  double best_eff = -1.0;
+  for (long long ns = 1; ns <= std::min<long long>(cap, 8 * cdiv(sms, tiles)); ++ns) {
+    const long long items = tiles * ns;
+    const long long waves = cdiv(items, sms);
+    const double eff = (double)items / (double)(waves * sms);
+    // prefer balance, then fewer splits (less split-K traffic)
+    if (eff > best_eff + 0.02) {
+      best_eff = eff;
+      best = ns;
+    }
+  }
+  return (int)best;
 }
 
 cudaError_t gemm_nt(const Planes& A, const Planes& B, double alpha, bool sym, bool accumulate,
@@ -600,6 +642,8 @@ cudaError_t gemm_nt(const Planes& A, const Planes& B, double alpha, bool sym, bo
   a.ntiles = tile_count(A.rows, B.rows, sym);
   a.nsplit = nsplit < 1 ? 1 : nsplit;
   a.kc_per_split = cdiv(A.nkc, a.nsplit);
+  // no split without K chunks: every split writes its partial sums
+  a.nsplit = (int)cdiv(A.nkc, a.kc_per_split);
   a.part = part;
   a.prow = (long long)a.tiles_m * kTileM;
   a.pcol = (long long)a.tiles_n * kTileN;

@@ -34,18 +34,18 @@ namespace oz {
 constexpr int kSlices = 7;          // digits per value (55 bits)
 constexpr int kTileM = 128;         // rows of A per tile (TMEM lanes)
 constexpr int kTileN = 64;          // rows of B per tile (TMEM columns per level)
-constexpr int kChunkK = 32;         // K per pipeline stage
+constexpr int kChunkK = 16;         // K per pipeline stage (one MMA per digit pair)
 constexpr int kBlockRows = 64;      // rows per pre-tiled block in global memory
 constexpr int kDrainK = 128;        // K accumulated per level before a drain
-constexpr int kBlockBytes = kBlockRows * kChunkK * 2;  // 4096: one slice of a 64-row block
+constexpr int kBlockElems = kBlockRows * kChunkK;  // 1024 bf16: one slice of a 64-row block
 
 // Pre-tiled slice planes of one operand.  plane s, K chunk kc, row block rb is
-// a 4096-byte block in the tensor cores' K-major no-swizzle layout: the 8x8
-// core matrix (row group i, K group j) at i * 512 + j * 128 bytes, row r of it
+// a 2048-byte block in the tensor cores' K-major no-swizzle layout: the 8x8
+// core matrix (row group i, K group j) at i * 256 + j * 128 bytes, row r of it
 // at r * 16 bytes.  Element offset (uint16) of (row, k, s):
-//   ((s * nkc + kc) * nrb + rb) * 2048 + i * 256 + j * 64 + r * 8 + (k % 8).
+//   ((s * nkc + kc) * nrb + rb) * 1024 + i * 128 + j * 64 + r * 8 + (k % 8).
 struct Planes {
-  uint16_t* d = nullptr;  // kSlices * nkc * nrb * 2048 values
+  uint16_t* d = nullptr;  // kSlices * nkc * nrb * 1024 values
   int* expo = nullptr;    // scale exponent per row (nrb * 64 entries)
   long long rows = 0, k = 0;
   long long nrb = 0, nkc = 0;

@@ -41,8 +41,10 @@ def _check(C, A, B):
     assert np.all(err <= bound), float(np.max(err / bound))
 
 
-@pytest.mark.parametrize("m,n,k", [(200, 200, 2000), (130, 70, 3000), (1, 1, 33), (129, 65, 31)])
+@pytest.mark.parametrize("m,n,k", [(200, 200, 2000), (130, 70, 3000), (1, 1, 33), (129, 65, 31),
+                                   (57, 57, 46656), (20, 9, 30000)])
 def test_gram_and_cross_products(m, n, k):
+    """Includes one-tile products with long K (split over every SM)."""
     rng = np.random.default_rng(m * 1000 + n)
     ctx = _ctx()
     A = _rows(rng, m, k)
@@ -78,3 +80,22 @@ def test_tensor_core_and_fp64_pipe_agree_at_subspace_sizes():
     ctx.set_subspace("tc")
     assert np.all(np.abs(tc - f64) <= 2 * _bound(A, A))
     assert np.all(np.abs(tcx - f64x) <= 2 * _bound(B, A))
+
+
+def test_repeatable_bit_for_bit_and_many_tiles_per_sm():
+    """Integer accumulation makes the result independent of scheduling: the
+    same products twice are bitwise equal.  A rotation with ~1000 output
+    tiles runs several tiles per SM through the same shared-memory stages."""
+    rng = np.random.default_rng(9)
+    ctx = _ctx()
+    A = _rows(rng, 160, 70000)
+    G1, G2 = ctx.subspace_gemm(A), ctx.subspace_gemm(A)
+    assert np.array_equal(G1, G2)
+    W = rng.standard_normal((300, 160))
+    X = _rows(rng, 160, 40000)
+    R1, R2 = ctx.subspace_rotate(W, X), ctx.subspace_rotate(W, X)
+    assert np.array_equal(R1, R2)
+    ctx.set_subspace("f64")
+    R64 = ctx.subspace_rotate(W, X)
+    ctx.set_subspace("tc")
+    assert np.all(np.abs(R1 - R64) <= 2 * _bound(W, X.T))
