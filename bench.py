@@ -51,11 +51,12 @@ def parse():
     p.add_argument("--batched", action="store_true",
                    help="32 uneven nanocrystals (48^3 .. 112^3) in one graph launch vs "
                         "32 sequential launches")
-    p.add_argument("--profile", choices=["mixed", "f64", "subspace"], default=None,
+    p.add_argument("--profile", choices=["mixed", "f64", "subspace", "pipeline"], default=None,
                    help="run only a small case for an ncu capture: 24 (mixed) or 16 "
                         "(f64) start states x 8 Newton steps of the 128^3 workload (3.5 GB "
                         "and 4.8 GB on the device), or (subspace) the tensor-core Gram of "
-                        "512 states x 262144 points (1.1 GB)")
+                        "512 states x 262144 points (1.1 GB)), or (pipeline) one whole mixed "
+                        "pipeline of the 128^3 workload for a launch list")
     return p.parse_args()
 
 
@@ -72,6 +73,15 @@ def run_profile(args):
             G = ctx.subspace_gemm(A)
         print(json.dumps({"profile_case": "subspace", "m": 512, "k": 1 << 18,
                           "checksum": float(np.trace(G))}))
+        return
+    if args.profile == "pipeline":
+        ctx = sep.Context(S.dims, S.steps, precision="mixed")
+        ctx.vbuild(S.xyz, S.types.astype(np.int32), tr, tv, [1024, 1024], S.mins)
+        start = sep.start_states(START_SEED, S.ns, S.ngrid, S.dv)
+        res = ctx.pipeline(start, S.el, S.nc, ctx.info()["vmin"])
+        print(json.dumps({"profile_case": "pipeline", "mkept": res["mkept"],
+                          "stages_s": {k: round(v, 3) for k, v in res["timing"].items()
+                                       if k.endswith("_s")}}))
         return
     ctx = sep.Context(S.dims, S.steps, precision=args.profile)
     ctx.set_block_steps(8)

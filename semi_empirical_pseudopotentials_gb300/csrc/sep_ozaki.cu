@@ -23,9 +23,10 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kStages = 4;
-constexpr int kSliceA = kTileM * kChunkK * 2;               // 4096 bytes
-constexpr int kSliceB = kTileN * kChunkK * 2;               // 2048 bytes
-constexpr int kStageBytes = kSlices * (kSliceA + kSliceB);  // 43008 bytes
+constexpr int kStageA = kSlices * kTileM * kChunkK * 2;    // 28672 bytes: one block
+constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 14336 bytes: half a block
+constexpr int kStageBytes = kStageA + kStageB;             // 43008 bytes
+constexpr uint32_t kRowGroupStride = kSlices * 256;        // bytes between 8-row groups
 constexpr int kTmemCols = 512;                              // kSlices * 64 = 448 used
 constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 8
 constexpr long long kSpin = 1LL << 26;                      // bounded waits
@@ -175,7 +176,8 @@ __device__ __forceinline__ uint32_t bf16_pair(int lo, int hi) {
 // element offset of (row block rb, K chunk kc, slice s) + position (rr, kk) in it
 __device__ __forceinline__ long long plane_off(int s, long long kc, long long rb, long long nkc,
                                                long long nrb, int rr, int kk) {
-  return ((s * nkc + kc) * nrb + rb) * kBlockElems + (rr >> 3) * (kChunkK * 8) + (kk >> 3) * 64 +
+  (void)nrb;
+  return (rb * nkc + kc) * kBlockElems + (((rr >> 3) * kSlices + s) * 2 + (kk >> 3)) * 64 +
          (rr & 7) * 8 + (kk & 7);
 }
 
@@ -379,13 +381,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
       const uint32_t base = smem0 + buf * kStageBytes;
       const uint32_t bar = smem_u32(&bar_load[buf]);
       mbar_expect_tx(bar, kStageBytes);
-#pragma unroll 1
-      for (int s = 0; s < kSlices; ++s) {
-        const uint16_t* sa = a.A + ((s * a.nkc + kc) * a.a_nrb + 2LL * tm) * kBlockElems;
-        const uint16_t* sb = a.B + ((s * a.nkc + kc) * a.b_nrb + tn) * kBlockElems;
-        bulk_g2s(base + s * kSliceA, sa, kSliceA, bar);
-        bulk_g2s(base + kSlices * kSliceA + s * kSliceB, sb, kSliceB, bar);
-      }
+      const uint16_t* sa = a.A + ((long long)tm * a.nkc + kc) * kBlockElems;
+      const uint16_t* sb =
+          a.B + ((long long)(tn >> 1) * a.nkc + kc) * kBlockElems + (tn & 1) * (kBlockElems / 2);
+      bulk_g2s(base, sa, kStageA, bar);
+      bulk_g2s(base + kStageA, sb, kStageB, bar);
       pending[buf] = true;
     };
 
@@ -407,11 +407,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
           const bool fresh = (st % kStagesPerDrain) == 0;
 #pragma unroll 1
           for (int s = 0; s < kSlices; ++s) {
-            const uint64_t da = smem_desc(base + s * kSliceA, 128, kChunkK * 16);
+            const uint64_t da = smem_desc(base + s * 256, 128, kRowGroupStride);
 #pragma unroll 1
             for (int t = 0; t < kSlices - s; ++t) {
-              const uint64_t db =
-                  smem_desc(base + kSlices * kSliceA + t * kSliceB, 128, kChunkK * 16);
+              const uint64_t db = smem_desc(base + kStageA + t * 256, 128, kRowGroupStride);
               mma_bf16(tmem + (uint32_t)((s + t) * kTileN), da, db, idesc,
                        (fresh && s == 0) ? 0u : 1u);
             }
@@ -534,7 +533,7 @@ namespace oz {
 
 namespace {
 long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
-long long padded_blocks(long long rows) { return 2 * cdiv(rows, kTileM); }  // 64-row blocks
+long long padded_blocks(long long rows) { return cdiv(rows, kBlockRows); }  // 128-row blocks
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
@@ -551,7 +550,7 @@ int tile_count(long long m, long long n, bool sym) {
 }  // namespace
 
 size_t plane_elems(long long rows, long long k) {
-  return (size_t)kSlices * (size_t)cdiv(k, kChunkK) * (size_t)padded_blocks(rows) * kBlockElems;
+  return (size_t)cdiv(k, kChunkK) * (size_t)padded_blocks(rows) * kBlockElems;
 }
 
 cudaError_t slice_rows(const double* X, long long rows, long long k, long long ld, Planes& p,

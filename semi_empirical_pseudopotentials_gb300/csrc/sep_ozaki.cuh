@@ -35,18 +35,22 @@ constexpr int kSlices = 7;          // digits per value (55 bits)
 constexpr int kTileM = 128;         // rows of A per tile (TMEM lanes)
 constexpr int kTileN = 64;          // rows of B per tile (TMEM columns per level)
 constexpr int kChunkK = 16;         // K per pipeline stage (one MMA per digit pair)
-constexpr int kBlockRows = 64;      // rows per pre-tiled block in global memory
+constexpr int kBlockRows = 128;     // rows per pre-tiled block in global memory
 constexpr int kDrainK = 128;        // K accumulated per level before a drain
-constexpr int kBlockElems = kBlockRows * kChunkK;  // 1024 bf16: one slice of a 64-row block
+constexpr int kBlockElems = kSlices * kBlockRows * kChunkK;  // 14336 bf16: all digits of a block
 
-// Pre-tiled slice planes of one operand.  plane s, K chunk kc, row block rb is
-// a 2048-byte block in the tensor cores' K-major no-swizzle layout: the 8x8
-// core matrix (row group i, K group j) at i * 256 + j * 128 bytes, row r of it
-// at r * 16 bytes.  Element offset (uint16) of (row, k, s):
-//   ((s * nkc + kc) * nrb + rb) * 1024 + i * 128 + j * 64 + r * 8 + (k % 8).
+// Pre-tiled digit planes of one operand.  Row block rb (128 rows) and K chunk
+// kc (16 values) hold all kSlices digits in one 28,672-byte block, in the
+// tensor cores' K-major no-swizzle layout with the digits interleaved: the 8x8
+// core matrix of digit s, row group i (0..15), K group j (0..1) at
+// ((i * kSlices + s) * 2 + j) * 128 bytes, row r of it at r * 16 bytes.  So a
+// block (or its first or second 64 rows) is one contiguous copy, and digit s of
+// it is a matrix with row-group stride kSlices * 256 bytes starting s * 256
+// bytes in.  Element offset (uint16) of (row rr of the block, k, digit s):
+//   (rb * nkc + kc) * 14336 + ((i * kSlices + s) * 2 + j) * 64 + r * 8 + (k % 8).
 struct Planes {
-  uint16_t* d = nullptr;  // kSlices * nkc * nrb * 1024 values
-  int* expo = nullptr;    // scale exponent per row (nrb * 64 entries)
+  uint16_t* d = nullptr;  // nrb * nkc * 14336 values
+  int* expo = nullptr;    // scale exponent per row (nrb * 128 entries)
   long long rows = 0, k = 0;
   long long nrb = 0, nkc = 0;
 };
