@@ -497,10 +497,11 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
   RET(ortho_device(c, d_psi, m, &k));
   RET(normalize_device(c, d_psi, k));  // main.c:112
   CK(cudaEventRecord(ev[3], c->stream));
-  RET(rayleigh_ritz_device(c, d_psi, k, eval));
-  RET(normalize_device(c, d_psi, k));  // main.c:122
+  double* hpsi = nullptr;  // H psi of the Ritz vectors, when it fits beside them
+  RET(rayleigh_ritz_device(c, d_psi, k, eval, &hpsi));
+  RET(normalize_device(c, d_psi, k, hpsi));  // main.c:122
   CK(cudaEventRecord(ev[4], c->stream));
-  RET(sigma_device(c, d_psi, k, sige));
+  RET(sigma_device(c, d_psi, k, sige, hpsi));
   CK(cudaEventRecord(ev[5], c->stream));
   if (psi_out)
     CK(cudaMemcpyAsync(psi_out, d_psi, sizeof(double) * (size_t)n * k, cudaMemcpyDeviceToHost,
@@ -518,7 +519,7 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
   t.mkept = k;
   t.dE = dE;
   t.dt = dt;
-  t.h_applies = (long)(t.power_iterations + 1) + (long)ns * (nc - 1) + 2 * k;
+  t.h_applies = (long)(t.power_iterations + 1) + (long)ns * (nc - 1) + (hpsi ? 1 : 2) * k;
   *mkept = k;
   if (timing) *timing = t;
   return kOk;

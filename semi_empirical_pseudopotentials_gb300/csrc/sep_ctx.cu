@@ -416,11 +416,12 @@ int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nst
                          reinterpret_cast<cx<double>*>(d_hpsi), nstates);
 }
 
-int normalize_device(sep_ctx* c, double* d_psi, long m) {
+int normalize_device(sep_ctx* c, double* d_psi, long m, double* also) {
   RET(grow(c, c->w_red, sizeof(double) * (reduce_partial_doubles(m) + (size_t)m + 64)));
   double* part = c->w_red.as<double>();
-  CK(normalize_rows<double>(d_psi, m, c->n, c->dv, part, part + reduce_partial_doubles(m),
-                            c->stream));
+  double* norms = part + reduce_partial_doubles(m);
+  CK(normalize_rows<double>(d_psi, m, c->n, c->dv, part, norms, c->stream));
+  if (also) CK(scale_rows<double>(also, m, c->n, norms, c->dv, c->stream));
   return kOk;
 }
 
@@ -623,30 +624,33 @@ int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept) {
 
 // filter/Hmat.c:11-86: H_ij = <H psi_i | psi_j> dv over the kept states, the
 // symmetric part diagonalised, psi rotated onto the eigenvectors.
-int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host) {
+int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host,
+                         double** hpsi) {
   const long long n = c->n;
   RET(grow(c, c->w_small, sizeof(double) * (4 * (size_t)m * m + 4 * (size_t)m)));
   double* A = c->w_small.as<double>();
   double* lam = A + (size_t)m * m;
-  double* At = lam + m;
-  // H psi for chunks of states, rows of A accumulated chunk by chunk
-  long long chunk = std::min<long long>(m, 256);
+  // H psi for chunks of states, rows of A accumulated chunk by chunk.  When
+  // H psi of all m states fits, it is kept and rotated with psi, so that sigma
+  // needs no further H applies (H is linear: H (V psi) = V (H psi)).
+  const size_t all = sizeof(double) * (size_t)n * (size_t)m;
+  const bool keep = hpsi && (all <= c->w_hpsi.bytes || all <= free_device_bytes() / 3);
+  long long chunk = keep ? m : std::min<long long>(m, 256);
   RET(grow(c, c->w_hpsi, sizeof(double) * (size_t)n * chunk));
   double* hps = c->w_hpsi.as<double>();
-  const size_t wd = gemm_nt_work_doubles(chunk, m, n);
-  RET(grow(c, c->w_gemm, sizeof(double) * wd));
   for (long long r0 = 0; r0 < m; r0 += chunk) {
     const long long rc = std::min<long long>(chunk, m - r0);
-    RET(apply_h_real(c, d_psi + r0 * n, hps, rc));
-    (void)wd;
-    RET(sub_gemm_nt(c, hps, d_psi, rc, m, n, c->dv, A + r0 * m, false));
+    double* h = keep ? hps + r0 * n : hps;
+    RET(apply_h_real(c, d_psi + r0 * n, h, rc));
+    RET(sub_gemm_nt(c, h, d_psi, rc, m, n, c->dv, A + r0 * m, false));
   }
-  (void)At;
   CK(symmetrize_f64(A, m, c->stream));
   RET(syevd(c, A, m, lam));
   // eigenvector j is column j (A[j*m + i]); new state j = sum_i V[i][j] psi_i
   // -> rotation matrix rows = columns of V = the col-major buffer read row-major
   RET(rotate_rows(c, d_psi, m, m, A));
+  if (keep) RET(rotate_rows(c, hps, m, m, A));
+  if (hpsi) *hpsi = keep ? hps : nullptr;
   CK(cudaMemcpyAsync(eval_host, lam, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return kOk;
@@ -654,10 +658,11 @@ int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host) {
 
 // filter/energy.c:88-119: sigma = sqrt(<H^2> - <H>^2) = |H psi - E psi| for a
 // normalised psi (dv metric) with E = <psi|H|psi>.
-int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host) {
+int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,
+                 const double* d_hpsi) {
   const long long n = c->n;
   long long chunk = std::min<long long>(m, 256);
-  RET(grow(c, c->w_hpsi, sizeof(double) * (size_t)n * chunk));
+  if (!d_hpsi) RET(grow(c, c->w_hpsi, sizeof(double) * (size_t)n * chunk));
   RET(grow(c, c->w_red, sizeof(double) * (reduce_partial_doubles(chunk) + 2 * (size_t)chunk + 64)));
   double* hps = c->w_hpsi.as<double>();
   double* part = c->w_red.as<double>();
@@ -665,9 +670,10 @@ int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host) {
   double* sg = e + chunk;
   for (long long r0 = 0; r0 < m; r0 += chunk) {
     const long long rc = std::min<long long>(chunk, m - r0);
-    RET(apply_h_real(c, d_psi + r0 * n, hps, rc));
-    CK(row_dots<double>(d_psi + r0 * n, hps, rc, n, c->dv, e, part, c->stream));
-    CK(residual_norms(d_psi + r0 * n, hps, e, rc, n, c->dv, sg, part, c->stream));
+    const double* h = d_hpsi ? d_hpsi + r0 * n : hps;
+    if (!d_hpsi) RET(apply_h_real(c, d_psi + r0 * n, hps, rc));
+    CK(row_dots<double>(d_psi + r0 * n, h, rc, n, c->dv, e, part, c->stream));
+    CK(residual_norms(d_psi + r0 * n, h, e, rc, n, c->dv, sg, part, c->stream));
     CK(cudaMemcpyAsync(sige_host + r0, sg, sizeof(double) * rc, cudaMemcpyDeviceToHost,
                        c->stream));
   }

@@ -93,9 +93,15 @@ int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nst
 int energy_all_device(sep_ctx* c, const double* d_psi, long m, double* ene_host);
 int energy_range_device(sep_ctx* c, double vmin, double* emax, double* dE, long* iters);
 int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept);
-int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host);
-int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host);
-int normalize_device(sep_ctx* c, double* d_psi, long m);
+// keep_hpsi: also return H psi of the rotated states (rotated with them) in
+// *hpsi when the device has room for it, else *hpsi = nullptr
+int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host,
+                         double** hpsi = nullptr);
+// d_hpsi: H psi of these states when already known (no H applies then)
+int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,
+                 const double* d_hpsi = nullptr);
+// also: rows scaled by the same factors as psi's (H psi follows psi)
+int normalize_device(sep_ctx* c, double* d_psi, long m, double* also = nullptr);
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out);
 int subspace_gemm_device(sep_ctx* c, const double* A, const double* B, long long m, long long n,
                          long long k, double alpha, bool sym, double* C);

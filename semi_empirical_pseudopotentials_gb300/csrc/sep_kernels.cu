@@ -477,6 +477,15 @@ cudaError_t normalize_rows(T* x, long long M, long long n, double dv, double* pa
   k_scale_rows<T><<<dim3(64, (unsigned)M), kThreads, 0, s>>>(x, n, norms_dev, dv);
   return cudaGetLastError();
 }
+template <typename T>
+cudaError_t scale_rows(T* x, long long M, long long n, const double* norms_dev, double dv,
+                       cudaStream_t s) {
+  if (M > 65535) return cudaErrorInvalidValue;
+  k_scale_rows<T><<<dim3(64, (unsigned)M), kThreads, 0, s>>>(x, n, norms_dev, dv);
+  return cudaGetLastError();
+}
+template cudaError_t scale_rows<double>(double*, long long, long long, const double*, double,
+                                        cudaStream_t);
 template cudaError_t normalize_rows<double>(double*, long long, long long, double, double*,
                                             double*, cudaStream_t);
 template cudaError_t normalize_rows<float>(float*, long long, long long, double, double*,

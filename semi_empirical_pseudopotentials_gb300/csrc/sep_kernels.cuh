@@ -39,6 +39,11 @@ template <typename T>
 cudaError_t normalize_rows(T* x, long long M, long long n, double dv, double* partial,
                            double* norms_dev, cudaStream_t s);
 size_t reduce_partial_doubles(long long rows);
+// x rows scaled by 1/sqrt(norms[m] * dv): the scaling of normalize_rows with
+// norms already computed (applied to a second array that must follow the first)
+template <typename T>
+cudaError_t scale_rows(T* x, long long M, long long n, const double* norms_dev, double dv,
+                       cudaStream_t s);
 
 // ---- FP64 contractions
 // C[m][n] = alpha * sum_k A[m][k] B[n][k]   (K contiguous in both; split over K,
