@@ -181,7 +181,7 @@ def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):
     """Compulsory HBM bytes of one launch (c: bytes per complex, r: per real)."""
     if kind in ("x_fwd", "y_fwd", "z_fki", "y_inv"):
         return 2 * c * n * npairs                      # read + write the grids
-    if kind == "x_inv_epi_fwd":
+    if kind in ("x_inv_epi_fwd", "xy_inv_epi_fwd"):
         return (4 * c) * n * npairs + r * n            # T in/out, psi_in, psi_out, V once
     if kind == "accumulate":
         return kblock * c * n * npairs + 2 * (2 * ms * r) * n * npairs
@@ -437,10 +437,14 @@ def run_sep(args):
     if not args.no_extras and rank == 0:
         peaks = measured_peaks()
         # roofline of the dominant kernel: per-launch device times of each kernel kind
-        names = ["x_fwd", "y_fwd", "z_fki", "y_inv", "x_inv_epi_fwd", "accumulate"]
+        names = ["x_fwd", "y_fwd", "z_fki", "y_inv", "x_inv_epi_fwd", "accumulate",
+                 "xy_inv_epi_fwd"]
         npairs = (ns + 1) // 2
         per = ctx.time_passes(npairs, reps=10)
-        launches = [1, nc - 1, nc - 1, nc - 1, nc - 1, (nc + 31) // 32]
+        if per[6] > 0:  # fused xy plane pass: z and xy passes per Newton step
+            launches = [0, 0, nc - 1, 0, 0, (nc + 31) // 32, nc]
+        else:
+            launches = [1, nc - 1, nc - 1, nc - 1, nc - 1, (nc + 31) // 32, 0]
         share = [p * l for p, l in zip(per, launches)]
         k = int(np.argmax(share))
         byts = algorithmic_bytes(names[k], npairs, n, 8, 4)
@@ -523,7 +527,10 @@ def run_sep(args):
         extras["cpu_baseline"] = cpu_baseline(S, pot, dE, an_re, zn, vmin)
 
     if rank == 0:
-        launches_step = 1 + 1 + 4 * (nc - 1) + (nc + 31) // 32 + 1
+        # pack, first forward transform, per Newton step 2 (fused xy plane pass,
+        # nx = ny = 128 in complex64) or 4 line passes, the accumulations, convert
+        fused = S.dims[0] == S.dims[1] and S.dims[0] in (64, 96, 128)
+        launches_step = 1 + 1 + (2 if fused else 4) * (nc - 1) + (nc + 31) // 32 + 1
         line = {"metric": "Hpsi applies/s at 128^3", "value": value, "unit": "applies/s",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,

@@ -70,6 +70,11 @@ int sep_ctx_stream(sep_ctx *ctx, void **cuda_stream);             /* cudaStream_
 int sep_ctx_set_graphs(sep_ctx *ctx, int enable);
 /* Newton steps accumulated per pass over the step history (default 32). */
 int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
+/* Complex64 Newton steps on grids with nx = ny in {64, 96, 128} use one fused
+ * pass per z-plane for the x and y transforms and the epilogue (two grid
+ * passes per step instead of four; same arithmetic per line).  enable = 0
+ * selects the four line passes.  Default 1. */
+int sep_ctx_set_fusion(sep_ctx *ctx, int enable);
 
 /* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------
  * hpsi = T psi + V psi for nstates complex grids (interleaved complex128). */
@@ -251,10 +256,12 @@ int sep_subspace_rotate(sep_ctx *ctx, const double *W, const double *X, long m, 
 /* ---- measurement --------------------------------------------------------
  * Average device time (ms, CUDA events on the context stream) of one launch
  * of each Newton-step kernel on npairs complex grids in the context's
- * precision, over reps launches each: ms_out[0..5] = x forward, y forward,
+ * precision, over reps launches each: ms_out[0..6] = x forward, y forward,
  * z forward*k^2*inverse, y inverse, x inverse+epilogue+forward, accumulate
- * (block_steps history grids into ms = 8 state pairs).  No counterpart in the
- * reference; used for the roofline report. */
+ * (block_steps history grids into ms = 8 state pairs), and the fused xy
+ * plane pass (y/x inverse + epilogue + x/y forward; 0 when the context does
+ * not use it).  No counterpart in the reference; used for the roofline
+ * report. */
 int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
 
 /* ---- normalisation that allocates nothing ------------------------------

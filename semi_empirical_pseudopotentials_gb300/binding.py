@@ -93,6 +93,7 @@ def lib():
         L.sep_ctx_set_tiles.argtypes = [vp, ip]
         L.sep_form_factor_backward.argtypes = [dp, C.c_double, dp, dp]
         L.sep_ctx_set_subspace.argtypes = [vp, C.c_int]
+        L.sep_ctx_set_fusion.argtypes = [vp, C.c_int]
         L.sep_subspace_gemm.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, C.c_double,
                                         C.c_int, dp]
         L.sep_subspace_rotate.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, dp]
@@ -333,8 +334,9 @@ class Context:
         _check(lib().sep_ctx_set_tiles(self.h, ch))
 
     def time_passes(self, npairs, reps=10):
-        """Average ms per launch: x fwd, y fwd, z fwd*k*inv, y inv, x inv+epi+fwd, accumulate."""
-        out = np.zeros(6)
+        """Average ms per launch: x fwd, y fwd, z fwd*k*inv, y inv, x inv+epi+fwd,
+        accumulate, and the fused xy plane pass (0 when it does not apply)."""
+        out = np.zeros(7)
         _check(lib().sep_time_passes(self.h, npairs, reps, _p(out)))
         return out
 
@@ -352,6 +354,10 @@ class Context:
                                 _p(tab_v), tab_n.ctypes.data_as(lp), tab_r.shape[1], _p(mins),
                                 _p(out), 1 if install else 0))
         return out
+
+    def set_fusion(self, enable):
+        """Fused xy plane pass for complex64 Newton steps (nx = ny in 64/96/128)."""
+        _check(lib().sep_ctx_set_fusion(self.h, 1 if enable else 0))
 
     def set_subspace(self, mode):
         """Subspace contractions on the tensor cores ("tc", default) or the FP64 pipe ("f64")."""

@@ -593,6 +593,12 @@ int sep_time_passes(sep_ctx* c, long npairs, int reps, double* ms_out) {
   return time_passes_device(c, npairs, reps, ms_out);
 }
 
+int sep_ctx_set_fusion(sep_ctx* c, int enable) {
+  if (!c) return arg_fail("null context");
+  c->fuse_xy = enable ? 1 : 0;
+  return kOk;
+}
+
 int sep_ctx_set_subspace(sep_ctx* c, int mode) {
   if (!c || (mode != 0 && mode != 1)) return arg_fail("sep_ctx_set_subspace: mode is 0 or 1");
   c->subspace_tc = mode;

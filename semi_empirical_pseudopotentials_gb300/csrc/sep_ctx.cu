@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "sep_ctx.cuh"
@@ -125,8 +126,16 @@ template <> struct Prec<float> {
   static GridDev<float>& grid(sep_ctx* c) { return c->g32; }
 };
 
+// the fused xy plane pass runs complex64 Newton steps on square xy planes
+template <typename T> bool use_xy(sep_ctx*) { return false; }
+template <> bool use_xy<float>(sep_ctx* c) { return c->fuse_xy && xy_supported(c->g32); }
+
+template <typename T>
+int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K);
+
 template <typename T>
 int newton_loop(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K) {
+  if (use_xy<T>(c)) return newton_loop_xy<T>(c, Bc, nstates, ms, nc, K);
   GridDev<T>& g = Prec<T>::grid(c);
   const long long n = c->n;
   cx<T>* hist = c->w_hist.as<cx<T>>();
@@ -159,6 +168,45 @@ int newton_loop(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K) 
   if (nc == 1)
     CK(newton_accumulate<T, T>(hist, K, Bc, n, 0, 1, an, nc, (int)ms, acc, nstates, true, s));
   return kOk;
+}
+
+// Newton loop with two passes per step: z (forward, k^2, inverse), then the
+// xy plane pass (y and x inverse, epilogue, x and y forward).  Same arithmetic
+// per line as the four line passes.
+template <typename T>
+int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K) {
+  if constexpr (!std::is_same<T, float>::value) {
+    return arg_fail("the xy plane pass is complex64 only");
+  } else {
+    GridDev<float>& g = c->g32;
+    const long long n = c->n;
+    cx<float>* hist = c->w_hist.as<cx<float>>();
+    const float* an = c->w_coef.as<float>();
+    cudaStream_t s = c->stream;
+    PassIO<float> io;
+    io.data = c->w_fft.as<cx<float>>();
+    io.src = hist;  // slot 0 = the start states
+    CK(run_xy_pass(kFwd, g, io, Bc, s));
+    io.src = nullptr;
+    io.coefs = c->w_steps.as<float>();
+    for (long j = 1; j < nc; ++j) {
+      CK(run_pass<float>(2, kFwdKInv, g, io, Bc, s));
+      io.psi_in = hist + (long long)((j - 1) % K) * Bc * n;
+      io.psi_out = hist + (long long)(j % K) * Bc * n;
+      io.step = (int)j;
+      CK(run_xy_pass((j + 1 < nc) ? kInvEpiFwd : kInvEpi, g, io, Bc, s));
+      if ((j + 1) % K == 0 || j == nc - 1) {
+        const long count = j % K + 1;
+        const long j0 = j - count + 1;
+        CK(newton_accumulate<float, float>(hist, K, Bc, n, j0, (int)count, an, nc, (int)ms,
+                                           c->w_acc.as<float>(), nstates, j0 == 0, s));
+      }
+    }
+    if (nc == 1)
+      CK(newton_accumulate<float, float>(hist, K, Bc, n, 0, 1, an, nc, (int)ms,
+                                         c->w_acc.as<float>(), nstates, true, s));
+    return kOk;
+  }
 }
 
 template <typename T>
@@ -197,6 +245,11 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
   }
+  const bool fused = use_xy<T>(c);
+  if (fused && !c->xy_ready) {  // kernel attributes, outside any stream capture
+    CK(xy_prepare(c->g32));
+    c->xy_ready = true;
+  }
   for (long long b0 = 0; b0 < B; b0 += Bc) {
     const int bc = (int)std::min<long long>(Bc, B - b0);
     const long long s0 = 2 * b0;
@@ -204,7 +257,8 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     CK(pack_pairs<T, double>(d_start + s0 * n, nst, n, c->w_hist.as<cx<T>>(), c->stream));
     if (c->use_graphs) {
       const long long key[8] = {bc, nst, ms, nc, K, (long long)(size_t)c->w_hist.p,
-                                (long long)(size_t)c->w_acc.p, (long long)sizeof(T)};
+                                (long long)(size_t)c->w_acc.p,
+                                (long long)sizeof(T) + (fused ? 256 : 0)};
       FilterGraph* hit = nullptr;
       for (auto& fg : c->graphs)
         if (std::memcmp(fg.key, key, sizeof key) == 0) hit = &fg;
@@ -701,10 +755,25 @@ template <typename T> int time_passes_impl(sep_ctx* c, long npairs, int reps, do
   CK(cudaEventCreate(&e1));
   const int axis[5] = {0, 1, 2, 1, 0};
   const int mode[5] = {kFwd, kFwd, kFwdKInv, kInv, kInvEpiFwd};
-  for (int k = 0; k < 6; ++k) {
+  const bool xy = use_xy<T>(c);
+  if (xy && !c->xy_ready) {
+    CK(xy_prepare(c->g32));
+    c->xy_ready = true;
+  }
+  ms_out[6] = 0.0;
+  for (int k = 0; k < (xy ? 7 : 6); ++k) {
     for (int r = -1; r < reps; ++r) {  // r = -1: warm-up
       if (r == 0) CK(cudaEventRecord(e0, c->stream));
-      if (k < 5) {
+      if (k == 6) {
+        if constexpr (std::is_same<T, float>::value) {
+          PassIO<float> p = io;
+          p.psi_in = hist;
+          p.psi_out = hist + (long long)n * npairs;
+          p.alpha = 0.1f;
+          p.beta = -0.5f;
+          CK(run_xy_pass(kInvEpiFwd, c->g32, p, (int)npairs, c->stream));
+        }
+      } else if (k < 5) {
         PassIO<T> p = io;
         if (k == 0) p.src = hist;
         if (k == 4) {

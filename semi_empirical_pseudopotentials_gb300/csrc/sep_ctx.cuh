@@ -73,6 +73,8 @@ struct sep_ctx {
   bool use_graphs = true;
   int block_steps = 32;
   int subspace_tc = 1;  // subspace contractions on the tensor cores (1) or the FP64 pipe (0)
+  int fuse_xy = 1;      // complex64 Newton steps with the fused xy plane pass when it applies
+  bool xy_ready = false;
   int batch_holds = 0;  // batches whose graph points at the filter workspace
   sep::host::KTables ktab;
   sep::GridDev<double> g64;

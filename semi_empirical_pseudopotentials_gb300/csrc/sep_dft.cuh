@@ -45,6 +45,15 @@ template <typename T> __device__ __forceinline__ cx<T> mulc(cx<T> a, cx<T> b) {
 template <int S, typename T> __device__ __forceinline__ cx<T> muli(cx<T> a) {
   return (S > 0) ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x);
 }
+// o = alpha (t + v p) + beta p, the Newton step's epilogue (filter/hnorm.c:11-39),
+// with its multiply-adds fixed so that every kernel rounds it the same way
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
+template <typename T>
+__device__ __forceinline__ cx<T> newton_epi(cx<T> t, T v, cx<T> p, T alpha, T beta) {
+  const T hx = fma_t(v, p.x, t.x), hy = fma_t(v, p.y, t.y);
+  return mk<T>(fma_t(alpha, hx, beta * p.x), fma_t(alpha, hy, beta * p.y));
+}
 template <typename T> __device__ __forceinline__ cx<T> scale(cx<T> a, T s) {
   return mk<T>(a.x * s, a.y * s);
 }

@@ -56,6 +56,13 @@ template <typename T>
 cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& io, int B,
                      cudaStream_t s);
 
+// Fused xy plane pass of a complex64 Newton step (sep_xypass.cuh): modes kFwd,
+// kInvEpi, kInvEpiFwd on whole z-planes; for nx = ny in {64, 96, 128}.
+bool xy_supported(const GridDev<float>& g);
+cudaError_t xy_prepare(const GridDev<float>& g);  // before any stream capture
+cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& io, int B,
+                        cudaStream_t s);
+
 // out = alpha (T x + V y) + beta y for B complex grids; y may be null (out = alpha T x).
 // scratch: B * n complex; out may not alias x.
 template <typename T>

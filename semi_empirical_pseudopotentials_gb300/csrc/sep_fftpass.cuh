@@ -39,6 +39,7 @@ template <typename T> struct PassArgs {
   cx<T>* psi_out;         // epilogue: new state
   const T* pot;           // epilogue: V on the grid (shared by the batch)
   const cx<T>* tw;        // exp(-2 pi i m / L), m < L, for this axis
+  const cx<T>* tw2;       // the same for the y axis (xy plane pass)
   const T* kx;            // k^2 axis tables, pre-scaled by 1/N (filter/init.c:125-135)
   const T* ky;
   const T* kz;
@@ -337,8 +338,7 @@ line_pass(PassArgs<T> a) {
           const int x = n1 + N1 * n2;
           const C p = pin ? pin[x] : mk<T>(T(0), T(0));
           const T v = pv[x];
-          C h = mk<T>(va[r][n2].x + v * p.x, va[r][n2].y + v * p.y);
-          C o = mk<T>(alpha * h.x + beta * p.x, alpha * h.y + beta * p.y);
+          const C o = newton_epi<T>(va[r][n2], v, p, alpha, beta);
           pout[x] = o;
           va[r][n2] = o;
         }

@@ -63,3 +63,21 @@ def test_autotuned_tile_shapes_give_identical_results(precision):
     assert len(choice) == 5 and set(choice) <= {0, 1}
     c = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
     assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("n", [64, 96, 128])
+def test_fused_xy_plane_pass_equals_the_line_passes(n):
+    """The complex64 Newton step with the fused xy plane pass does the same
+    arithmetic per line as the four line passes: the filters are equal."""
+    dims = (n, n, 16 if n == 128 else 24)
+    ctx, pot, dv, npts = _job(dims, 3, "mixed")
+    vmin = float(pot.min())
+    nc, dE = 70, 40.0
+    ar, ai, zn = sep.coefficients([-1.0, -0.6, -0.2], nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+    start = sep.start_states(-11, 5, npts, dv)
+    fused = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    ctx.set_fusion(False)
+    lines = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    ctx.set_fusion(True)
+    d = np.abs(fused - lines).max()
+    assert np.array_equal(fused, lines), (d, d / np.abs(lines).max())
