@@ -859,6 +859,10 @@ int autotune_device(sep_ctx* c, long npairs, int reps, int* choice) {
 // job's Newton loop as a parallel branch, so a single launch runs them all.
 namespace {
 template <typename T> int batch_job_prepare(sep_ctx* c, long ns, long ms, long nc) {
+  if (use_xy<T>(c) && !c->xy_ready) {  // kernel attributes, before the batch capture
+    CK(xy_prepare(c->g32));
+    c->xy_ready = true;
+  }
   const long long n = c->n;
   int K = c->block_steps;
   if (K > nc) K = (int)nc;
