@@ -174,7 +174,9 @@ def subspace_gram(sep, ctx, psi_d, m, n, dv, peaks):
 TRAFFIC_PER_PAIR_128 = {"y_fwd": (201.354752e6 + 142.915584e6) / 12,
                         "z_fki": (201.357312e6 + 140.684032e6) / 12,
                         "y_inv": (201.346304e6 + 143.166208e6) / 12,
-                        "x_inv_epi_fwd": (444.561152e6 + 351.911936e6) / 12}
+                        "x_inv_epi_fwd": (444.561152e6 + 351.911936e6) / 12,
+                        # profiles/xy_plane_pass_c64_128.md (12 pairs)
+                        "xy_inv_epi_fwd": (411.152384e6 + 346.868992e6) / 12}
 
 
 def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):
