@@ -286,12 +286,7 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
       RET(newton_loop<T>(c, bc, nst, ms, nc, K));
     }
     double* dst = d_out + s0 * ms * n;
-    if (sizeof(T) == sizeof(double)) {
-      CK(cudaMemcpyAsync(dst, c->w_acc.p, sizeof(double) * (size_t)nst * ms * n,
-                         cudaMemcpyDeviceToDevice, c->stream));
-    } else {
-      CK(convert_f32_to_f64(c->w_acc.as<float>(), dst, nst * ms * n, c->stream));
-    }
+    CK(unpack_accumulators<T>(c->w_acc.as<T>(), bc, n, (int)ms, nst, dst, c->stream));
   }
   return kOk;
 }
@@ -884,11 +879,7 @@ int batch_job_capture(sep_ctx* c, const double* d_start, long ns, long ms, long 
   const int B = (int)((ns + 1) / 2);
   CK(pack_pairs<T, double>(d_start, ns, n, c->w_hist.as<cx<T>>(), c->stream));
   RET(newton_loop<T>(c, B, ns, ms, nc, K));
-  if (sizeof(T) == sizeof(double))
-    CK(cudaMemcpyAsync(d_out, c->w_acc.p, sizeof(double) * (size_t)ns * ms * n,
-                       cudaMemcpyDeviceToDevice, c->stream));
-  else
-    CK(convert_f32_to_f64(c->w_acc.as<float>(), d_out, (long long)ns * ms * n, c->stream));
+  CK(unpack_accumulators<T>(c->w_acc.as<T>(), B, n, (int)ms, ns, d_out, c->stream));
   return kOk;
 }
 

@@ -2,6 +2,8 @@
 // contractions (see sep_kernels.cuh).
 #include "sep_kernels.cuh"
 
+#include <type_traits>
+
 namespace sep {
 
 namespace {
@@ -44,6 +46,7 @@ __global__ void k_unpack(const cx<T>* __restrict__ in, long long nstates, long l
 
 // -------------------------------------------------------------------------
 constexpr int kMaxBlockSteps = 64;  // history grids per accumulation pass
+constexpr int kLoadBatch = 8;       // history loads in flight per thread (ms > 4)
 
 template <typename T, typename TA, int MSMAX>
 __global__ void __launch_bounds__(kThreads)
@@ -62,16 +65,33 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
   for (int s = threadIdx.x; s < count; s += blockDim.x)
     soff[s] = (long long)((j0 + s) % slots) * ((long long)B * n) + b * n;
   __syncthreads();
-  const long long s0 = 2 * b, s1 = 2 * b + 1;
-  const bool two = s1 < nstates;
-  TA* __restrict__ a0 = acc + s0 * ms * n;
-  TA* __restrict__ a1 = acc + s1 * ms * n;
+  (void)nstates;  // the imaginary half of an odd last pair is zero and unread
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
        g += (long long)gridDim.x * blockDim.x) {
     TA re[MSMAX], im[MSMAX];
 #pragma unroll
     for (int e = 0; e < MSMAX; ++e) { re[e] = TA(0); im[e] = TA(0); }
-    for (int s = 0; s < count; ++s) {
+    // LB history loads are issued before their products, so each thread
+    // keeps that many grid loads in flight
+    constexpr int LB = MSMAX >= 8 ? kLoadBatch : kLoadBatch / 2;
+    int s = 0;
+    for (; s + LB <= count; s += LB) {
+      cx<T> h[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u) h[u] = hist[soff[s + u] + g];
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+#pragma unroll
+        for (int e = 0; e < MSMAX; ++e) {
+          if (e < ms) {
+            const TA c = cf[e * kMaxBlockSteps + s + u];
+            re[e] += c * (TA)h[u].x;
+            im[e] += c * (TA)h[u].y;
+          }
+        }
+      }
+    }
+    for (; s < count; ++s) {
       const cx<T> h = hist[soff[s] + g];
 #pragma unroll
       for (int e = 0; e < MSMAX; ++e) {
@@ -82,16 +102,67 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
         }
       }
     }
+    // the 2 ms accumulators of (pair b, point g) are adjacent: targets of
+    // state 2b, then of state 2b + 1
+    TA* __restrict__ pa = acc + (b * n + g) * (2 * ms);
+    if (std::is_same<TA, float>::value && MSMAX <= 16 && ms == MSMAX) {
+      float4* p4 = reinterpret_cast<float4*>(pa);
 #pragma unroll
-    for (int e = 0; e < MSMAX; ++e) {
-      if (e < ms) {
-        TA* p0 = a0 + e * n + g;
-        *p0 = init ? re[e] : *p0 + re[e];
-        if (two) {
-          TA* p1 = a1 + e * n + g;
-          *p1 = init ? im[e] : *p1 + im[e];
+      for (int q = 0; q < MSMAX / 2; ++q) {
+        TA v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = 4 * q + u;
+          v[u] = k < MSMAX ? re[k] : im[k - MSMAX];
+        }
+        float4 o = make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+        if (!init) {
+          const float4 old = p4[q];
+          o = make_float4(old.x + o.x, old.y + o.y, old.z + o.z, old.w + o.w);
+        }
+        p4[q] = o;
+      }
+    } else if (std::is_same<TA, float>::value && ms % 2 == 0) {
+      float2* q0 = reinterpret_cast<float2*>(pa);
+      float2* q1 = reinterpret_cast<float2*>(pa + ms);
+#pragma unroll
+      for (int e = 0; e < MSMAX; e += 2) {
+        if (e < ms) {
+          float2 r = make_float2((float)re[e], (float)re[e + 1]);
+          float2 i = make_float2((float)im[e], (float)im[e + 1]);
+          if (!init) {
+            const float2 r0 = q0[e / 2], i0 = q1[e / 2];
+            r = make_float2(r0.x + r.x, r0.y + r.y);
+            i = make_float2(i0.x + i.x, i0.y + i.y);
+          }
+          q0[e / 2] = r;
+          q1[e / 2] = i;
         }
       }
+    } else {
+#pragma unroll
+      for (int e = 0; e < MSMAX; ++e) {
+        if (e < ms) {
+          pa[e] = init ? re[e] : pa[e] + re[e];
+          pa[ms + e] = init ? im[e] : pa[ms + e] + im[e];
+        }
+      }
+    }
+  }
+}
+
+// accumulators [B][n][2 ms] -> out[(2b + c) ms + e][g] (state-major, double)
+template <typename TA>
+__global__ void k_unpack_acc(const TA* __restrict__ acc, long long B, long long n, int ms,
+                             long long nstates, double* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < B * n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long b = i / n, g = i - b * n;
+    const TA* pa = acc + i * (2 * ms);
+    for (int c = 0; c < 2; ++c) {
+      const long long st = 2 * b + c;
+      if (st >= nstates) break;
+      for (int e = 0; e < ms; ++e) out[(st * ms + e) * n + g] = (double)pa[c * ms + e];
     }
   }
 }
@@ -440,6 +511,18 @@ template cudaError_t newton_accumulate<float, float>(const cx<float>*, int, int,
                                                      long long, int, const float*, long long,
                                                      int, float*, long long, bool,
                                                      cudaStream_t);
+
+template <typename TA>
+cudaError_t unpack_accumulators(const TA* acc, long long B, long long n, int ms,
+                                long long nstates, double* out, cudaStream_t s) {
+  k_unpack_acc<TA><<<blocks_for(B * n, kThreads, 152LL * 16), kThreads, 0, s>>>(acc, B, n, ms,
+                                                                                 nstates, out);
+  return cudaGetLastError();
+}
+template cudaError_t unpack_accumulators<float>(const float*, long long, long long, int,
+                                                long long, double*, cudaStream_t);
+template cudaError_t unpack_accumulators<double>(const double*, long long, long long, int,
+                                                 long long, double*, cudaStream_t);
 
 size_t reduce_partial_doubles(long long rows) { return (size_t)rows * kPartials * 2; }
 

@@ -18,12 +18,18 @@ cudaError_t unpack_pairs(const cx<T>* in, long long nstates, long long n, TR* re
                          cudaStream_t s);
 
 // ---- Newton accumulation (filter/filter.c:60-78), blocked over K steps:
-//   acc[(2b+c) ms + e][g] (+)= sum_{s<count} an[e nc + j0 + s] * comp_c(hist[slot(j0+s)][b][g])
-// hist is a ring of `slots` grids [slots][B][n]; slot(j) = j % slots.
+//   acc[b][g][c ms + e] (+)= sum_{s<count} an[e nc + j0 + s] * comp_c(hist[slot(j0+s)][b][g])
+// hist is a ring of `slots` grids [slots][B][n]; slot(j) = j % slots.  The 2 ms
+// accumulators of a point are adjacent; unpack_accumulators writes them out
+// state-major, out[(2b + c) ms + e][g] as double (the reference's psitot).
 template <typename T, typename TA>
 cudaError_t newton_accumulate(const cx<T>* hist, int slots, int B, long long n, long long j0,
                               int count, const TA* an, long long nc, int ms, TA* acc,
                               long long nstates, bool init, cudaStream_t s);
+
+template <typename TA>
+cudaError_t unpack_accumulators(const TA* acc, long long B, long long n, int ms,
+                                long long nstates, double* out, cudaStream_t s);
 
 // ---- reductions (FP64 sums, deterministic two-level)
 // complex pairs: out[b] = (sum x.re y.re, sum x.im y.im) * w
