@@ -39,6 +39,8 @@ template <typename T> void free_grid(GridDev<T>& g) {
   if (g.kx) cudaFree(g.kx);
   if (g.ky) cudaFree(g.ky);
   if (g.kz) cudaFree(g.kz);
+  if (g.kxr) cudaFree(g.kxr);
+  if (g.kyr) cudaFree(g.kyr);
   if (g.pot) cudaFree(g.pot);
   g = GridDev<T>();
 }
@@ -63,6 +65,18 @@ template <typename T> int upload_grid(sep_ctx* c, GridDev<T>& g) {
     CK(cudaMemcpy(*dst[a], kt.data(), sizeof(T) * kt.size(), cudaMemcpyHostToDevice));
   }
   g.kcap = (T)c->ktab.cap;
+  const int n1 = (c->nx == c->ny && sizeof(T) == sizeof(float)) ? xy_split_n1((int)c->nx) : 0;
+  if (n1 > 0) {  // x and y tables in the plane pass's position order
+    const int L = (int)c->nx, n2 = L / n1;
+    const std::vector<double>* kxy[2] = {&c->ktab.kx, &c->ktab.ky};
+    T** dr[2] = {&g.kxr, &g.kyr};
+    for (int a = 0; a < 2; ++a) {
+      std::vector<T> kt(L);
+      for (int p = 0; p < L; ++p) kt[p] = (T)(*kxy[a])[(p / n1) + n2 * (p % n1)];
+      CK(cudaMalloc(dr[a], sizeof(T) * L));
+      CK(cudaMemcpy(*dr[a], kt.data(), sizeof(T) * L, cudaMemcpyHostToDevice));
+    }
+  }
   CK(cudaMalloc(&g.pot, sizeof(T) * c->n));
   CK(cudaMemset(g.pot, 0, sizeof(T) * c->n));
   return kOk;

@@ -178,7 +178,10 @@ int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int 
   if constexpr (!std::is_same<T, float>::value) {
     return arg_fail("the xy plane pass is complex64 only");
   } else {
-    GridDev<float>& g = c->g32;
+    const GridDev<float>& g = c->g32;
+    GridDev<float> gz = g;  // the z pass sees x and y in the plane pass's order
+    gz.kx = g.kxr;
+    gz.ky = g.kyr;
     const long long n = c->n;
     cx<float>* hist = c->w_hist.as<cx<float>>();
     const float* an = c->w_coef.as<float>();
@@ -190,7 +193,7 @@ int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int 
     io.src = nullptr;
     io.coefs = c->w_steps.as<float>();
     for (long j = 1; j < nc; ++j) {
-      CK(run_pass<float>(2, kFwdKInv, g, io, Bc, s));
+      CK(run_pass<float>(2, kFwdKInv, gz, io, Bc, s));
       io.psi_in = hist + (long long)((j - 1) % K) * Bc * n;
       io.psi_out = hist + (long long)(j % K) * Bc * n;
       io.step = (int)j;

@@ -26,6 +26,10 @@ template <typename T> struct GridDev {
   T kcap = 0;
   T* pot = nullptr;
   int variant[5] = {0, 0, 0, 0, 0};  // tile shape per pass kind (autotuned)
+  // k^2 axis tables in the xy plane pass's digit-reversed position order
+  // (complex64 grids with nx = ny in {64, 96, 128}; else null)
+  T* kxr = nullptr;
+  T* kyr = nullptr;
 };
 
 // pass kinds of a Newton step: x forward, y forward, z forward*k^2*inverse,
@@ -58,6 +62,10 @@ cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& i
 
 // Fused xy plane pass of a complex64 Newton step (sep_xypass.cuh): modes kFwd,
 // kInvEpi, kInvEpiFwd on whole z-planes; for nx = ny in {64, 96, 128}.
+// Between xy plane passes x and y are kept in digit-reversed position order:
+// element k = k2 + N2 k1 of an axis of length L = N1 N2 at position k1 + N1 k2,
+// N1 = xy_split_n1(L) (0: no plane pass for L).
+int xy_split_n1(int L);
 bool xy_supported(const GridDev<float>& g);
 cudaError_t xy_prepare(const GridDev<float>& g);  // before any stream capture
 cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& io, int B,

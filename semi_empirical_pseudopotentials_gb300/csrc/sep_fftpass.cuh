@@ -39,7 +39,6 @@ template <typename T> struct PassArgs {
   cx<T>* psi_out;         // epilogue: new state
   const T* pot;           // epilogue: V on the grid (shared by the batch)
   const cx<T>* tw;        // exp(-2 pi i m / L), m < L, for this axis
-  const cx<T>* tw2;       // the same for the y axis (xy plane pass)
   const T* kx;            // k^2 axis tables, pre-scaled by 1/N (filter/init.c:125-135)
   const T* ky;
   const T* kz;

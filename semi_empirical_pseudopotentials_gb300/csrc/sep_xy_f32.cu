@@ -6,27 +6,27 @@ namespace sep {
 
 namespace {
 
-template <int L> constexpr size_t xy_smem() {
-  return (size_t)L * (L + 1) * sizeof(cx<float>) + 2 * (size_t)L * sizeof(cx<float>);
-}
-
 template <int L, int MODE>
 cudaError_t launch_xy(const PassArgs<float>& a, int B, cudaStream_t s) {
   if (a.nz > 65535 || B < 1) return cudaErrorInvalidValue;
-  xy_plane_pass<L, L, MODE><<<dim3((unsigned)B, (unsigned)a.nz), kXyThreads, xy_smem<L>(), s>>>(a);
+  xy_plane_pass<L, MODE>
+      <<<dim3((unsigned)B, (unsigned)a.nz), kXyThreads, XyShape<L>::smem_bytes, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int L> cudaError_t prepare_len() {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(xy_plane_pass<L, L, kFwd>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xy_smem<L>())))
+  if ((e = cudaFuncSetAttribute(xy_plane_pass<L, kFwd>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)XyShape<L>::smem_bytes)))
     return e;
-  if ((e = cudaFuncSetAttribute(xy_plane_pass<L, L, kInvEpi>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xy_smem<L>())))
+  if ((e = cudaFuncSetAttribute(xy_plane_pass<L, kInvEpi>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)XyShape<L>::smem_bytes)))
     return e;
-  return cudaFuncSetAttribute(xy_plane_pass<L, L, kInvEpiFwd>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xy_smem<L>());
+  return cudaFuncSetAttribute(xy_plane_pass<L, kInvEpiFwd>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)XyShape<L>::smem_bytes);
 }
 
 template <int L>
@@ -39,8 +39,15 @@ cudaError_t launch_mode(int mode, const PassArgs<float>& a, int B, cudaStream_t 
 
 }  // namespace
 
+int xy_split_n1(int L) {
+  if (L == 64) return Split<64>::n1;
+  if (L == 96) return Split<96>::n1;
+  if (L == 128) return Split<128>::n1;
+  return 0;
+}
+
 bool xy_supported(const GridDev<float>& g) {
-  return g.nx == g.ny && (g.nx == 64 || g.nx == 96 || g.nx == 128);
+  return g.nx == g.ny && xy_split_n1(g.nx) > 0 && g.kxr && g.kyr;
 }
 
 cudaError_t xy_prepare(const GridDev<float>& g) {
@@ -61,7 +68,6 @@ cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& 
   a.step = io.step;
   a.pot = g.pot;
   a.tw = g.tw[0];
-  a.tw2 = g.tw[1];
   a.alpha = io.alpha;
   a.beta = io.beta;
   a.nx = g.nx;

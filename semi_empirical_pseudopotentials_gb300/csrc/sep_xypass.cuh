@@ -9,11 +9,23 @@
 //   (filter/hnorm.c:11-39), x forward, y forward
 // so the grid is read and written once less per step.
 //
-// Each 1-D transform is the four-step split of sep_fftpass.cuh, with the same
-// register DFTs and twiddles in the same order, run in place on the plane:
-// lines are the rows (x transforms) or the columns (y transforms).  The row
-// stride is nx + 1 elements, so that 32 threads on 32 different rows, or on 32
-// adjacent columns, touch 32 different bank pairs.
+// Transforms.  Each 1-D transform of length L = N1 N2 is the four-step split
+// of sep_fftpass.cuh, with the same register DFTs and twiddles in the same
+// order, done in place and self-sorting: every item writes its results back to
+// the positions it read.  The forward transform then leaves element
+//   k = k2 + N2 k1   at position   k1 + N1 k2
+// and the inverse transform takes its input in that order and leaves natural
+// order.  Between passes the grids are therefore kept with x and y in this
+// digit-reversed position order (z natural); the z pass looks k^2 up through
+// tables in the same order, so every element sees the same arithmetic as with
+// the line passes.  The epilogue (psi_{j-1}, V, psi_j) runs in natural order.
+//
+// Passes over shared memory.  The first y stage reads the plane from global
+// memory and the last one writes it there; x inverse stage A', the epilogue
+// and x forward stage A work on the same items and share one pass.  The row
+// stride is L + 1 elements, so that the threads of a half-warp on 16
+// different rows, or on 16 adjacent columns, touch different bank pairs.
+// The block's plane, psi_{j-1} and V are prefetched into L2 when it starts.
 #pragma once
 
 #include "sep_fftpass.cuh"
@@ -22,189 +34,280 @@ namespace sep {
 
 constexpr int kXyThreads = 512;
 
-// forward (SIGN -1) or inverse (SIGN +1) transform of NL lines of length L in
-// place, natural order in and out; line l starts at l * LS, element e of a
-// line at e * ES
-template <int L, int SIGN, int NL, int LS, int ES>
-__device__ __forceinline__ void plane_fft(cx<float>* pl, const cx<float>* tws) {
-  using C = cx<float>;
-  constexpr int N1 = Split<L>::n1, N2 = Split<L>::n2;
-  constexpr int NA = NL * N1, NB = NL * N2;
-  constexpr int NT = kXyThreads;
-  const int tid = threadIdx.x;
-  if constexpr (SIGN < 0) {
-    // stage A: item (line, x1): elements x1 + N1 x2 -> DFT_N2, twiddle; the
-    // results go back to the positions the item read
-    for (int i = tid; i < NA; i += NT) {
-      const int line = i % NL, x1 = i / NL;
-      C* p = pl + line * LS;
-      C v[N2];
-#pragma unroll
-      for (int x2 = 0; x2 < N2; ++x2) v[x2] = p[(x1 + N1 * x2) * ES];
-      Dft<N2, -1, float>::run(v);
-#pragma unroll
-      for (int k2 = 1; k2 < N2; ++k2) v[k2] = mul<float>(v[k2], tws[(x1 * k2) % L]);
-#pragma unroll
-      for (int k2 = 0; k2 < N2; ++k2) p[(x1 + N1 * k2) * ES] = v[k2];
-    }
-    __syncthreads();
-    // stage B: item (line, k2): positions x1 + N1 k2 -> DFT_N1 -> element k2 + N2 k1
-    constexpr int IB = (NB + NT - 1) / NT;
-    C w[IB][N1];
-#pragma unroll
-    for (int r = 0; r < IB; ++r) {
-      const int i = tid + r * NT;
-      if (NB % NT == 0 || i < NB) {
-        const int line = i % NL, k2 = i / NL;
-        const C* p = pl + line * LS;
-#pragma unroll
-        for (int x1 = 0; x1 < N1; ++x1) w[r][x1] = p[(x1 + N1 * k2) * ES];
-        Dft<N1, -1, float>::run(w[r]);
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < IB; ++r) {
-      const int i = tid + r * NT;
-      if (NB % NT == 0 || i < NB) {
-        const int line = i % NL, k2 = i / NL;
-        C* p = pl + line * LS;
-#pragma unroll
-        for (int k1 = 0; k1 < N1; ++k1) p[(k2 + N2 * k1) * ES] = w[r][k1];
-      }
-    }
-    __syncthreads();
-  } else {
-    // stage B': item (line, k2): elements k2 + N2 k1 -> inverse DFT_N1,
-    // conjugate twiddle; back to the positions the item read
-    for (int i = tid; i < NB; i += NT) {
-      const int line = i % NL, k2 = i / NL;
-      C* p = pl + line * LS;
-      C v[N1];
-#pragma unroll
-      for (int k1 = 0; k1 < N1; ++k1) v[k1] = p[(k2 + N2 * k1) * ES];
-      Dft<N1, +1, float>::run(v);
-#pragma unroll
-      for (int n1 = 1; n1 < N1; ++n1) v[n1] = mulc<float>(v[n1], tws[(n1 * k2) % L]);
-#pragma unroll
-      for (int n1 = 0; n1 < N1; ++n1) p[(k2 + N2 * n1) * ES] = v[n1];
-    }
-    __syncthreads();
-    // stage A': item (line, n1): positions k2 + N2 n1 -> inverse DFT_N2 ->
-    // element n1 + N1 n2
-    constexpr int IA = (NA + NT - 1) / NT;
-    C u[IA][N2];
-#pragma unroll
-    for (int r = 0; r < IA; ++r) {
-      const int i = tid + r * NT;
-      if (NA % NT == 0 || i < NA) {
-        const int line = i % NL, n1 = i / NL;
-        const C* p = pl + line * LS;
-#pragma unroll
-        for (int k2 = 0; k2 < N2; ++k2) u[r][k2] = p[(k2 + N2 * n1) * ES];
-        Dft<N2, +1, float>::run(u[r]);
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < IA; ++r) {
-      const int i = tid + r * NT;
-      if (NA % NT == 0 || i < NA) {
-        const int line = i % NL, n1 = i / NL;
-        C* p = pl + line * LS;
-#pragma unroll
-        for (int n2 = 0; n2 < N2; ++n2) p[(n1 + N1 * n2) * ES] = u[r][n2];
-      }
-    }
-    __syncthreads();
+template <int L> struct XyShape {
+  static constexpr int n1 = Split<L>::n1, n2 = Split<L>::n2;
+  static constexpr int rs = L + 1;  // row stride (elements)
+  static_assert(n1 == 8 && L % 16 == 0, "row groups of the epilogue step");
+  static constexpr size_t smem_bytes = ((size_t)L * rs + L) * sizeof(cx<float>);
+};
+
+namespace xy {
+
+using C = cx<float>;
+
+// bulk L2 prefetch of [p, p + bytes) (16-byte aligned, bytes a multiple of
+// 16) in 16 KB pieces, one per lane of the calling warp
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes, int lane) {
+  constexpr unsigned kPiece = 16384;
+  for (unsigned o = (unsigned)lane * kPiece; o < bytes; o += 32 * kPiece) {
+    const unsigned n = bytes - o < kPiece ? bytes - o : kPiece;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char*)p + o), "r"(n)
+                 : "memory");
   }
 }
 
-// One block per (grid of the batch, z-plane), the grids of one plane adjacent
-// so that the plane of V is read from L2 after its first use.  MODE: kFwd (x
-// and y forward of src, or of data), kInvEpi (y and x inverse + epilogue),
-// kInvEpiFwd (and the forward transforms of the result).  Global accesses
-// move two neighbouring x values at a time, eight per thread in flight.
-template <int LX, int LY, int MODE>
-__global__ void __launch_bounds__(kXyThreads, 1) xy_plane_pass(PassArgs<float> a) {
-  using C = cx<float>;
-  constexpr int RS = LX + 1;
-  static_assert(LX % 2 == 0, "pairs of neighbouring x values");
-  constexpr int NP = LX * LY / 2;                  // pairs of x values in a plane
-  constexpr bool WHOLE = NP % (8 * kXyThreads) == 0;  // batches of 8 pairs per thread
-  extern __shared__ __align__(16) unsigned char xy_smem[];
-  C* pl = reinterpret_cast<C*>(xy_smem);
-  C* twx = pl + LY * RS;
-  C* twy = twx + LX;
-  const int tid = threadIdx.x;
-  const long long N = (long long)LX * LY * a.nz;
-  const long long goff = (long long)blockIdx.y * LX * LY;  // offset in one grid
-  const long long off = (long long)blockIdx.x * N + goff;
-  for (int m = tid; m < LX; m += kXyThreads) twx[m] = a.tw[m];
-  for (int m = tid; m < LY; m += kXyThreads) twy[m] = a.tw2[m];
-  const C* src = (MODE == kFwd && a.src) ? a.src : a.data;
-  {
-    const float4* s4 = reinterpret_cast<const float4*>(src + off);
-    for (int q0 = tid; q0 < NP; q0 += 8 * kXyThreads) {
-      float4 v[8];
+// row of group j of an x stage whose items are spread over N1 = 8 threads:
+// the two rows of a half-warp are 8 apart (16 banks apart with stride L + 1)
+__device__ __forceinline__ int row_of_group(int j) {
+  return (j & ~15) | ((j & 1) << 3) | ((j >> 1) & 7);
+}
+
+// ---- y transforms: lines are the columns (element stride RS)
+
+// inverse stage B' from global memory (g: the plane in position order, row
+// stride L): item (column, k2): positions k1 + N1 k2 -> inverse DFT_N1,
+// conjugate twiddle, back to the same positions in shared memory.  Adjacent
+// threads on adjacent columns; two items per thread loaded before either is
+// transformed.
+template <int L>
+__device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __restrict__ g) {
+  using S = XyShape<L>;
+  constexpr int NI = L * S::n2;
+  for (int i0 = threadIdx.x; i0 < NI; i0 += 2 * kXyThreads) {
+    C v[2][S::n1];
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
-        if (WHOLE || q0 + u * kXyThreads < NP) v[u] = s4[q0 + u * kXyThreads];
+    for (int t = 0; t < 2; ++t) {
+      const int i = i0 + t * kXyThreads;
+      if (NI % (2 * kXyThreads) == 0 || i < NI) {
+        const int col = i % L, k2 = i / L;
+        const C* q = g + (long long)(S::n1 * k2) * L + col;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (!WHOLE && q0 + u * kXyThreads >= NP) break;
-        const int i = 2 * (q0 + u * kXyThreads);
-        C* q = pl + (i / LX) * RS + (i % LX);
-        q[0] = mk<float>(v[u].x, v[u].y);
-        q[1] = mk<float>(v[u].z, v[u].w);
+        for (int k1 = 0; k1 < S::n1; ++k1) v[t][k1] = q[(long long)k1 * L];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int i = i0 + t * kXyThreads;
+      if (NI % (2 * kXyThreads) == 0 || i < NI) {
+        const int col = i % L, k2 = i / L;
+        Dft<S::n1, +1, float>::run(v[t]);
+#pragma unroll
+        for (int n1 = 1; n1 < S::n1; ++n1) v[t][n1] = mulc<float>(v[t][n1], tw[(n1 * k2) % L]);
+        C* p = pl + S::n1 * k2 * S::rs + col;
+#pragma unroll
+        for (int n1 = 0; n1 < S::n1; ++n1) p[n1 * S::rs] = v[t][n1];
       }
     }
   }
+}
+
+// inverse stage A': item (column, n1): positions n1 + N1 k2 -> inverse DFT_N2;
+// element n1 + N1 n2 at its natural position
+template <int L> __device__ __forceinline__ void col_inv_a(C* pl) {
+  using S = XyShape<L>;
+  for (int i = threadIdx.x; i < L * S::n1; i += kXyThreads) {
+    const int col = i % L, n1 = i / L;
+    C* p = pl + n1 * S::rs + col;
+    C u[S::n2];
+#pragma unroll
+    for (int k2 = 0; k2 < S::n2; ++k2) u[k2] = p[S::n1 * k2 * S::rs];
+    Dft<S::n2, +1, float>::run(u);
+#pragma unroll
+    for (int n2 = 0; n2 < S::n2; ++n2) p[S::n1 * n2 * S::rs] = u[n2];
+  }
+}
+
+// forward stage A: item (column, x1): positions x1 + N1 x2 -> DFT_N2, twiddle
+template <int L> __device__ __forceinline__ void col_fwd_a(C* pl, const C* tw) {
+  using S = XyShape<L>;
+  for (int i = threadIdx.x; i < L * S::n1; i += kXyThreads) {
+    const int col = i % L, x1 = i / L;
+    C* p = pl + x1 * S::rs + col;
+    C v[S::n2];
+#pragma unroll
+    for (int x2 = 0; x2 < S::n2; ++x2) v[x2] = p[S::n1 * x2 * S::rs];
+    Dft<S::n2, -1, float>::run(v);
+#pragma unroll
+    for (int k2 = 1; k2 < S::n2; ++k2) v[k2] = mul<float>(v[k2], tw[(x1 * k2) % L]);
+#pragma unroll
+    for (int k2 = 0; k2 < S::n2; ++k2) p[S::n1 * k2 * S::rs] = v[k2];
+  }
+}
+
+// forward stage B to global memory: item (column, k2): positions x1 + N1 k2
+// -> DFT_N1; element k2 + N2 k1 to position k1 + N1 k2 of g
+template <int L> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __restrict__ g) {
+  using S = XyShape<L>;
+  for (int i = threadIdx.x; i < L * S::n2; i += kXyThreads) {
+    const int col = i % L, k2 = i / L;
+    const C* p = pl + S::n1 * k2 * S::rs + col;
+    C w[S::n1];
+#pragma unroll
+    for (int x1 = 0; x1 < S::n1; ++x1) w[x1] = p[x1 * S::rs];
+    Dft<S::n1, -1, float>::run(w);
+    C* q = g + (long long)(S::n1 * k2) * L + col;
+#pragma unroll
+    for (int k1 = 0; k1 < S::n1; ++k1) q[(long long)k1 * L] = w[k1];
+  }
+}
+
+// ---- x transforms: lines are the rows
+
+// inverse stage B': item (row, k2): positions k1 + N1 k2 (elements k2 + N2 k1)
+// -> inverse DFT_N1, conjugate twiddle
+template <int L> __device__ __forceinline__ void row_inv_b(C* pl, const C* tw) {
+  using S = XyShape<L>;
+  for (int i = threadIdx.x; i < L * S::n2; i += kXyThreads) {
+    const int row = i % L, k2 = i / L;
+    C* p = pl + row * S::rs + S::n1 * k2;
+    C v[S::n1];
+#pragma unroll
+    for (int k1 = 0; k1 < S::n1; ++k1) v[k1] = p[k1];
+    Dft<S::n1, +1, float>::run(v);
+#pragma unroll
+    for (int n1 = 1; n1 < S::n1; ++n1) v[n1] = mulc<float>(v[n1], tw[(n1 * k2) % L]);
+#pragma unroll
+    for (int n1 = 0; n1 < S::n1; ++n1) p[n1] = v[n1];
+  }
+}
+
+// forward stage B: item (row, k2): positions x1 + N1 k2 -> DFT_N1; element
+// k2 + N2 k1 stays at position k1 + N1 k2
+template <int L> __device__ __forceinline__ void row_fwd_b(C* pl) {
+  using S = XyShape<L>;
+  for (int i = threadIdx.x; i < L * S::n2; i += kXyThreads) {
+    const int row = i % L, k2 = i / L;
+    C* p = pl + row * S::rs + S::n1 * k2;
+    C w[S::n1];
+#pragma unroll
+    for (int x1 = 0; x1 < S::n1; ++x1) w[x1] = p[x1];
+    Dft<S::n1, -1, float>::run(w);
+#pragma unroll
+    for (int k1 = 0; k1 < S::n1; ++k1) p[k1] = w[k1];
+  }
+}
+
+// x inverse stage A', the Newton epilogue and (FWD) x forward stage A in one
+// step: item (row, n1) holds the natural elements n1 + N1 n2 of its row, which
+// are also the inputs of forward item (row, x1 = n1).  psi_{j-1}, V and psi_j
+// (plane offsets off in the batch, goff in one grid) are accessed at those
+// elements: eight threads cover N1 = 8 adjacent elements (64 bytes) of a row.
+template <int L, bool FWD>
+__device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs<float>& a,
+                                              long long off, long long goff, float alpha,
+                                              float beta) {
+  using S = XyShape<L>;
+  constexpr int NCH = 4;  // the epilogue in chunks of N2 / 4 elements
+  static_assert(S::n2 % NCH == 0, "epilogue chunks");
+  constexpr int HN = S::n2 / NCH;
+  const C* __restrict__ pin = a.psi_in ? a.psi_in + off : nullptr;
+  const float* __restrict__ pv = a.pot + goff;
+  C* __restrict__ pout = a.psi_out + off;
+  for (int i = threadIdx.x; i < L * 8; i += kXyThreads) {
+    const int n1 = i & 7, row = row_of_group(i >> 3);
+    const long long g0 = (long long)row * L + n1;
+    C* p = pl + row * S::rs + n1;
+    C u[S::n2];
+#pragma unroll
+    for (int k2 = 0; k2 < S::n2; ++k2) u[k2] = p[S::n1 * k2];
+    Dft<S::n2, +1, float>::run(u);
+#pragma unroll
+    for (int h = 0; h < NCH; ++h) {
+      C q[HN];
+      float v[HN];
+#pragma unroll
+      for (int m = 0; m < HN; ++m) {
+        const long long e = g0 + S::n1 * (h * HN + m);
+        q[m] = pin ? pin[e] : mk<float>(0.f, 0.f);
+        v[m] = pv[e];
+      }
+#pragma unroll
+      for (int m = 0; m < HN; ++m) {
+        const int n2 = h * HN + m;
+        const C o = newton_epi<float>(u[n2], v[m], q[m], alpha, beta);
+        pout[g0 + S::n1 * n2] = o;
+        u[n2] = o;
+      }
+    }
+    if constexpr (FWD) {
+      Dft<S::n2, -1, float>::run(u);
+#pragma unroll
+      for (int k2 = 1; k2 < S::n2; ++k2) u[k2] = mul<float>(u[k2], tw[(n1 * k2) % L]);
+#pragma unroll
+      for (int k2 = 0; k2 < S::n2; ++k2) p[S::n1 * k2] = u[k2];
+    }
+  }
+}
+
+// x forward stage A from global memory (natural order): item (row, x1)
+template <int L>
+__device__ __forceinline__ void row_fwd_a_from(C* pl, const C* tw, const C* __restrict__ g) {
+  using S = XyShape<L>;
+  for (int i = threadIdx.x; i < L * 8; i += kXyThreads) {
+    const int x1 = i & 7, row = row_of_group(i >> 3);
+    const C* q = g + (long long)row * L + x1;
+    C v[S::n2];
+#pragma unroll
+    for (int x2 = 0; x2 < S::n2; ++x2) v[x2] = q[S::n1 * x2];
+    Dft<S::n2, -1, float>::run(v);
+#pragma unroll
+    for (int k2 = 1; k2 < S::n2; ++k2) v[k2] = mul<float>(v[k2], tw[(x1 * k2) % L]);
+    C* p = pl + row * S::rs + x1;
+#pragma unroll
+    for (int k2 = 0; k2 < S::n2; ++k2) p[S::n1 * k2] = v[k2];
+  }
+}
+
+}  // namespace xy
+
+// One block per (grid of the batch, z-plane), the grids of one plane adjacent
+// so that the plane of V is read from L2 after its first use.  MODE: kFwd (x
+// and y forward of src, or of data, natural order in), kInvEpi (y and x
+// inverse + epilogue), kInvEpiFwd (and the forward transforms of the result).
+template <int L, int MODE>
+__global__ void __launch_bounds__(kXyThreads, 1) xy_plane_pass(PassArgs<float> a) {
+  using C = cx<float>;
+  using S = XyShape<L>;
+  extern __shared__ __align__(16) unsigned char xy_smem[];
+  C* pl = reinterpret_cast<C*>(xy_smem);
+  C* tw = pl + L * S::rs;
+  const int tid = threadIdx.x;
+  const long long N = (long long)L * L * a.nz;
+  const long long goff = (long long)blockIdx.y * L * L;  // offset in one grid
+  const long long off = (long long)blockIdx.x * N + goff;
+  const C* src = (MODE == kFwd && a.src) ? a.src : a.data;
+  if (tid < 32) {  // the plane, psi_{j-1} and V into L2
+    xy::prefetch_l2(src + off, (unsigned)(L * L * sizeof(C)), tid);
+    if (MODE != kFwd) {
+      if (a.psi_in) xy::prefetch_l2(a.psi_in + off, (unsigned)(L * L * sizeof(C)), tid);
+      xy::prefetch_l2(a.pot + goff, (unsigned)(L * L * sizeof(float)), tid);
+    }
+  }
+  for (int m = tid; m < L; m += kXyThreads) tw[m] = a.tw[m];  // x and y tables are equal
   __syncthreads();
-  if constexpr (MODE != kFwd) {
-    plane_fft<LY, +1, LX, 1, RS>(pl, twy);  // y inverse: lines are the columns
-    plane_fft<LX, +1, LY, RS, 1>(pl, twx);  // x inverse: lines are the rows
+  if constexpr (MODE == kFwd) {
+    xy::row_fwd_a_from<L>(pl, tw, src + off);  // x forward
+  } else {
+    xy::col_inv_b_from<L>(pl, tw, a.data + off);  // y inverse
+    __syncthreads();
+    xy::col_inv_a<L>(pl);
+    __syncthreads();
+    xy::row_inv_b<L>(pl, tw);  // x inverse, epilogue (and x forward stage A)
+    __syncthreads();
     float alpha = a.alpha, beta = a.beta;
     if (a.coefs) {
       alpha = a.coefs[2 * a.step];
       beta = a.coefs[2 * a.step + 1];
     }
-    const float4* pin = a.psi_in ? reinterpret_cast<const float4*>(a.psi_in + off) : nullptr;
-    const float2* pv = reinterpret_cast<const float2*>(a.pot + goff);
-    float4* pout = reinterpret_cast<float4*>(a.psi_out + off);
-    for (int q0 = tid; q0 < NP; q0 += 8 * kXyThreads) {
-      float4 p[8];
-      float2 v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (WHOLE || q0 + u * kXyThreads < NP) {
-          p[u] = pin ? pin[q0 + u * kXyThreads] : make_float4(0.f, 0.f, 0.f, 0.f);
-          v[u] = pv[q0 + u * kXyThreads];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (!WHOLE && q0 + u * kXyThreads >= NP) break;
-        const int i = 2 * (q0 + u * kXyThreads);
-        C* q = pl + (i / LX) * RS + (i % LX);
-        const C o0 = newton_epi<float>(q[0], v[u].x, mk<float>(p[u].x, p[u].y), alpha, beta);
-        const C o1 = newton_epi<float>(q[1], v[u].y, mk<float>(p[u].z, p[u].w), alpha, beta);
-        pout[q0 + u * kXyThreads] = make_float4(o0.x, o0.y, o1.x, o1.y);
-        q[0] = o0;
-        q[1] = o1;
-      }
-    }
-    __syncthreads();
+    xy::row_inv_a_epi<L, MODE == kInvEpiFwd>(pl, tw, a, off, goff, alpha, beta);
   }
   if constexpr (MODE != kInvEpi) {
-    plane_fft<LX, -1, LY, RS, 1>(pl, twx);  // x forward
-    plane_fft<LY, -1, LX, 1, RS>(pl, twy);  // y forward
-    float4* d4 = reinterpret_cast<float4*>(a.data + off);
-    for (int q = tid; q < NP; q += kXyThreads) {
-      const int i = 2 * q;
-      const C* r = pl + (i / LX) * RS + (i % LX);
-      d4[q] = make_float4(r[0].x, r[0].y, r[1].x, r[1].y);
-    }
+    __syncthreads();
+    xy::row_fwd_b<L>(pl);
+    __syncthreads();
+    xy::col_fwd_a<L>(pl, tw);  // y forward
+    __syncthreads();
+    xy::col_fwd_b_to<L>(pl, a.data + off);
   }
 }
 
