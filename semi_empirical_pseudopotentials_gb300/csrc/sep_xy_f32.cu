@@ -6,11 +6,26 @@ namespace sep {
 
 namespace {
 
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      n = 152;
+  }
+  return n;
+}
+
 template <int L, int MODE>
 cudaError_t launch_xy(const PassArgs<float>& a, int B, cudaStream_t s) {
   if (a.nz > 65535 || B < 1) return cudaErrorInvalidValue;
-  xy_plane_pass<L, MODE>
-      <<<dim3((unsigned)B, (unsigned)a.nz), kXyThreads, XyShape<L>::smem_bytes, s>>>(a);
+  // 96^2 and 128^2 planes: one block per SM walks its planes; 64^2 planes
+  // (three blocks per SM) take one block each
+  const long long planes = (long long)B * a.nz;
+  if (planes > 0x7fffffffLL) return cudaErrorInvalidValue;
+  const int grid = (L <= 64 || planes < sm_count()) ? (int)planes : sm_count();
+  xy_plane_pass<L, MODE><<<grid, XyShape<L>::nt, XyShape<L>::smem_bytes, s>>>(a, B);
   return cudaGetLastError();
 }
 

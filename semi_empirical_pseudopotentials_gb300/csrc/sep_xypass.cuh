@@ -25,18 +25,21 @@
 // and x forward stage A work on the same items and share one pass.  The row
 // stride is L + 1 elements, so that the threads of a half-warp on 16
 // different rows, or on 16 adjacent columns, touch different bank pairs.
-// The block's plane, psi_{j-1} and V are prefetched into L2 when it starts.
+// Each block prefetches its next plane, psi_{j-1} and V into L2 while it
+// transforms the current one.
 #pragma once
 
 #include "sep_fftpass.cuh"
 
 namespace sep {
 
-constexpr int kXyThreads = 512;
-
 template <int L> struct XyShape {
   static constexpr int n1 = Split<L>::n1, n2 = Split<L>::n2;
   static constexpr int rs = L + 1;  // row stride (elements)
+  // threads per block and blocks per SM: a 64^2 plane (33 KB) leaves room
+  // for three blocks per SM
+  static constexpr int nt = L <= 64 ? 256 : 512;
+  static constexpr int min_blocks = L <= 64 ? 3 : 1;
   static_assert(n1 == 8 && L % 16 == 0, "row groups of the epilogue step");
   static constexpr size_t smem_bytes = ((size_t)L * rs + L) * sizeof(cx<float>);
 };
@@ -73,12 +76,12 @@ template <int L>
 __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __restrict__ g) {
   using S = XyShape<L>;
   constexpr int NI = L * S::n2;
-  for (int i0 = threadIdx.x; i0 < NI; i0 += 2 * kXyThreads) {
+  for (int i0 = threadIdx.x; i0 < NI; i0 += 2 * S::nt) {
     C v[2][S::n1];
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
-      const int i = i0 + t * kXyThreads;
-      if (NI % (2 * kXyThreads) == 0 || i < NI) {
+      const int i = i0 + t * S::nt;
+      if (NI % (2 * S::nt) == 0 || i < NI) {
         const int col = i % L, k2 = i / L;
         const C* q = g + (long long)(S::n1 * k2) * L + col;
 #pragma unroll
@@ -87,8 +90,8 @@ __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __re
     }
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
-      const int i = i0 + t * kXyThreads;
-      if (NI % (2 * kXyThreads) == 0 || i < NI) {
+      const int i = i0 + t * S::nt;
+      if (NI % (2 * S::nt) == 0 || i < NI) {
         const int col = i % L, k2 = i / L;
         Dft<S::n1, +1, float>::run(v[t]);
 #pragma unroll
@@ -105,7 +108,7 @@ __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __re
 // element n1 + N1 n2 at its natural position
 template <int L> __device__ __forceinline__ void col_inv_a(C* pl) {
   using S = XyShape<L>;
-  for (int i = threadIdx.x; i < L * S::n1; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * S::n1; i += S::nt) {
     const int col = i % L, n1 = i / L;
     C* p = pl + n1 * S::rs + col;
     C u[S::n2];
@@ -120,7 +123,7 @@ template <int L> __device__ __forceinline__ void col_inv_a(C* pl) {
 // forward stage A: item (column, x1): positions x1 + N1 x2 -> DFT_N2, twiddle
 template <int L> __device__ __forceinline__ void col_fwd_a(C* pl, const C* tw) {
   using S = XyShape<L>;
-  for (int i = threadIdx.x; i < L * S::n1; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * S::n1; i += S::nt) {
     const int col = i % L, x1 = i / L;
     C* p = pl + x1 * S::rs + col;
     C v[S::n2];
@@ -138,7 +141,7 @@ template <int L> __device__ __forceinline__ void col_fwd_a(C* pl, const C* tw) {
 // -> DFT_N1; element k2 + N2 k1 to position k1 + N1 k2 of g
 template <int L> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __restrict__ g) {
   using S = XyShape<L>;
-  for (int i = threadIdx.x; i < L * S::n2; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * S::n2; i += S::nt) {
     const int col = i % L, k2 = i / L;
     const C* p = pl + S::n1 * k2 * S::rs + col;
     C w[S::n1];
@@ -157,7 +160,7 @@ template <int L> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __
 // -> inverse DFT_N1, conjugate twiddle
 template <int L> __device__ __forceinline__ void row_inv_b(C* pl, const C* tw) {
   using S = XyShape<L>;
-  for (int i = threadIdx.x; i < L * S::n2; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * S::n2; i += S::nt) {
     const int row = i % L, k2 = i / L;
     C* p = pl + row * S::rs + S::n1 * k2;
     C v[S::n1];
@@ -175,7 +178,7 @@ template <int L> __device__ __forceinline__ void row_inv_b(C* pl, const C* tw) {
 // k2 + N2 k1 stays at position k1 + N1 k2
 template <int L> __device__ __forceinline__ void row_fwd_b(C* pl) {
   using S = XyShape<L>;
-  for (int i = threadIdx.x; i < L * S::n2; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * S::n2; i += S::nt) {
     const int row = i % L, k2 = i / L;
     C* p = pl + row * S::rs + S::n1 * k2;
     C w[S::n1];
@@ -203,7 +206,7 @@ __device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs
   const C* __restrict__ pin = a.psi_in ? a.psi_in + off : nullptr;
   const float* __restrict__ pv = a.pot + goff;
   C* __restrict__ pout = a.psi_out + off;
-  for (int i = threadIdx.x; i < L * 8; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * 8; i += S::nt) {
     const int n1 = i & 7, row = row_of_group(i >> 3);
     const long long g0 = (long long)row * L + n1;
     C* p = pl + row * S::rs + n1;
@@ -243,7 +246,7 @@ __device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs
 template <int L>
 __device__ __forceinline__ void row_fwd_a_from(C* pl, const C* tw, const C* __restrict__ g) {
   using S = XyShape<L>;
-  for (int i = threadIdx.x; i < L * 8; i += kXyThreads) {
+  for (int i = threadIdx.x; i < L * 8; i += S::nt) {
     const int x1 = i & 7, row = row_of_group(i >> 3);
     const C* q = g + (long long)row * L + x1;
     C v[S::n2];
@@ -260,12 +263,17 @@ __device__ __forceinline__ void row_fwd_a_from(C* pl, const C* tw, const C* __re
 
 }  // namespace xy
 
-// One block per (grid of the batch, z-plane), the grids of one plane adjacent
-// so that the plane of V is read from L2 after its first use.  MODE: kFwd (x
-// and y forward of src, or of data, natural order in), kInvEpi (y and x
-// inverse + epilogue), kInvEpiFwd (and the forward transforms of the result).
+// Block b of the grid walks the planes p = b + k gridDim.x of the batch (one
+// block per SM, or one block per plane), plane p = (z, grid b) with z = p / B, b = p % B, so that the
+// blocks running at one time share the plane of V.  After its epilogue a
+// block prefetches the data of its next plane into L2, so that the plane's
+// HBM reads overlap the forward transforms of this one; psi_{j-1} and V are
+// prefetched when the plane starts.
+// MODE: kFwd (x and y forward of src, or of data, natural order in),
+// kInvEpi (y and x inverse + epilogue), kInvEpiFwd (and the forward
+// transforms of the result).
 template <int L, int MODE>
-__global__ void __launch_bounds__(kXyThreads, 1) xy_plane_pass(PassArgs<float> a) {
+__global__ void __launch_bounds__(XyShape<L>::nt, XyShape<L>::min_blocks) xy_plane_pass(PassArgs<float> a, int B) {
   using C = cx<float>;
   using S = XyShape<L>;
   extern __shared__ __align__(16) unsigned char xy_smem[];
@@ -273,41 +281,53 @@ __global__ void __launch_bounds__(kXyThreads, 1) xy_plane_pass(PassArgs<float> a
   C* tw = pl + L * S::rs;
   const int tid = threadIdx.x;
   const long long N = (long long)L * L * a.nz;
-  const long long goff = (long long)blockIdx.y * L * L;  // offset in one grid
-  const long long off = (long long)blockIdx.x * N + goff;
+  const long long planes = (long long)B * a.nz;
   const C* src = (MODE == kFwd && a.src) ? a.src : a.data;
-  if (tid < 32) {  // the plane, psi_{j-1} and V into L2
-    xy::prefetch_l2(src + off, (unsigned)(L * L * sizeof(C)), tid);
-    if (MODE != kFwd) {
+  // the plane's data (prefetch distance: from the epilogue of the block's
+  // previous plane), and its psi_{j-1} and V (from the start of the plane)
+  auto prefetch_data = [&](long long p) {
+    if (tid < 32 && p < planes)
+      xy::prefetch_l2(src + (p % B) * N + (p / B) * L * L, (unsigned)(L * L * sizeof(C)), tid);
+  };
+  auto prefetch_epi = [&](long long p) {
+    if (MODE != kFwd && tid < 32) {
+      const long long goff = (p / B) * L * L, off = (p % B) * N + goff;
       if (a.psi_in) xy::prefetch_l2(a.psi_in + off, (unsigned)(L * L * sizeof(C)), tid);
       xy::prefetch_l2(a.pot + goff, (unsigned)(L * L * sizeof(float)), tid);
     }
+  };
+  prefetch_data(blockIdx.x);
+  for (int m = tid; m < L; m += S::nt) tw[m] = a.tw[m];  // x and y tables are equal
+  float alpha = a.alpha, beta = a.beta;
+  if (a.coefs) {
+    alpha = a.coefs[2 * a.step];
+    beta = a.coefs[2 * a.step + 1];
   }
-  for (int m = tid; m < L; m += kXyThreads) tw[m] = a.tw[m];  // x and y tables are equal
-  __syncthreads();
-  if constexpr (MODE == kFwd) {
-    xy::row_fwd_a_from<L>(pl, tw, src + off);  // x forward
-  } else {
-    xy::col_inv_b_from<L>(pl, tw, a.data + off);  // y inverse
-    __syncthreads();
-    xy::col_inv_a<L>(pl);
-    __syncthreads();
-    xy::row_inv_b<L>(pl, tw);  // x inverse, epilogue (and x forward stage A)
-    __syncthreads();
-    float alpha = a.alpha, beta = a.beta;
-    if (a.coefs) {
-      alpha = a.coefs[2 * a.step];
-      beta = a.coefs[2 * a.step + 1];
+  for (long long p = blockIdx.x; p < planes; p += gridDim.x) {
+    prefetch_epi(p);
+    const long long goff = (p / B) * L * L;  // offset in one grid
+    const long long off = (p % B) * N + goff;
+    __syncthreads();  // the previous plane's last stage has read the plane
+    if constexpr (MODE == kFwd) {
+      xy::row_fwd_a_from<L>(pl, tw, src + off);  // x forward
+    } else {
+      xy::col_inv_b_from<L>(pl, tw, a.data + off);  // y inverse
+      __syncthreads();
+      xy::col_inv_a<L>(pl);
+      __syncthreads();
+      xy::row_inv_b<L>(pl, tw);  // x inverse, epilogue (and x forward stage A)
+      __syncthreads();
+      xy::row_inv_a_epi<L, MODE == kInvEpiFwd>(pl, tw, a, off, goff, alpha, beta);
     }
-    xy::row_inv_a_epi<L, MODE == kInvEpiFwd>(pl, tw, a, off, goff, alpha, beta);
-  }
-  if constexpr (MODE != kInvEpi) {
-    __syncthreads();
-    xy::row_fwd_b<L>(pl);
-    __syncthreads();
-    xy::col_fwd_a<L>(pl, tw);  // y forward
-    __syncthreads();
-    xy::col_fwd_b_to<L>(pl, a.data + off);
+    prefetch_data(p + gridDim.x);
+    if constexpr (MODE != kInvEpi) {
+      __syncthreads();
+      xy::row_fwd_b<L>(pl);
+      __syncthreads();
+      xy::col_fwd_a<L>(pl, tw);  // y forward
+      __syncthreads();
+      xy::col_fwd_b_to<L>(pl, a.data + off);
+    }
   }
 }
 
