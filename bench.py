@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--batched", action="store_true",
                    help="32 uneven nanocrystals (48^3 .. 112^3) in one graph launch vs "
                         "32 sequential launches")
+    p.add_argument("--large", action="store_true",
+                   help="one whole mixed pipeline on the 4 nm sphere: 192^3 grid, 256 start "
+                        "states x 8 targets (about 250 GB on the device)")
     p.add_argument("--profile", choices=["mixed", "f64", "subspace", "pipeline"], default=None,
                    help="run only a small case for an ncu capture: 24 (mixed) or 16 "
                         "(f64) start states x 8 Newton steps of the 128^3 workload (3.5 GB "
@@ -630,12 +633,69 @@ def run_batched(args):
     batch.close()
 
 
+def run_large(args):
+    """The large mixed-precision run: 4 nm CdSe-like sphere, 192^3 grid, 256
+    start states x 8 targets, nc = 1024.  The complex64 filter's output (2048
+    FP64 states, 116 GB) and ortho's second block of the same size share the
+    device with the filter's workspaces, which the pipeline frees before ortho
+    when the device is short.  One pipeline after a small warm-up; device
+    memory in use is sampled with nvidia-smi every 200 ms."""
+    import subprocess
+
+    import torch
+
+    import semi_empirical_pseudopotentials_gb300 as sep
+    from semi_empirical_pseudopotentials_gb300 import systems
+
+    S = systems.make_system("r4.0nm_192", 4.0, 192, 8, 256, 1024, seed=11, elmin=-3.25,
+                            elmax=-2.95)
+    tr, tv = tables(sep, S)
+    warm_pipeline(sep)
+    ctx = sep.Context(S.dims, S.steps, precision="mixed")
+    ctx.vbuild(S.xyz, S.types.astype(np.int32), tr, tv, [1024, 1024], S.mins)
+    vmin = ctx.info()["vmin"]
+    start = sep.start_states(START_SEED, S.ns, S.ngrid, S.dv)
+    idx = torch.cuda.current_device()
+    smi = subprocess.Popen(["nvidia-smi", f"--id={idx}", "--query-gpu=memory.used,memory.total",
+                            "--format=csv,noheader,nounits", "-lms", "200"],
+                           stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    t0 = time.perf_counter()
+    res = ctx.pipeline(start, S.el, S.nc, vmin)
+    wall = time.perf_counter() - t0
+    smi.terminate()
+    out, _ = smi.communicate()
+    used = [tuple(float(x) for x in ln.split(",")) for ln in out.splitlines() if "," in ln]
+    t = res["timing"]
+    ev, sg = res["eval"], res["sigma"]
+    inwin = (ev >= S.el[0]) & (ev <= S.el[-1])
+    line = {"metric": "whole mixed pipeline, 4 nm sphere at 192^3", "unit": "s",
+            "value": t["total_s"], "higher_is_better": False, "n_gpus": 1, "dtype": "c64+f64",
+            "data": "synthetic",
+            "config": {"workload": f"r4.0nm CdSe-like sphere ({S.natom} atoms), 192^3 "
+                                   f"({S.ngrid} points), {S.ns} start states x {S.ms} targets, "
+                                   f"nc {S.nc}",
+                       "precision": "complex64 filter, FP32 accumulation; FP64 ortho and "
+                                    "Rayleigh-Ritz"},
+            "stages_s": {k: round(v, 3) for k, v in t.items() if k.endswith("_s")},
+            "wall_s": wall,
+            "filter_applies_per_s": S.ns * (S.nc - 1) / t["filter_s"],
+            "mkept": res["mkept"], "in_window": int(inwin.sum()),
+            "median_sigma_in_window": float(np.median(sg[inwin])) if inwin.any() else None,
+            "device_memory_used_gib": {"peak": max(u[0] for u in used) / 1024 if used else None,
+                                       "total": used[0][1] / 1024 if used else None,
+                                       "samples": len(used)}}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.profile:
         run_profile(args)
     elif args.batched:
         run_batched(args)
+    elif args.large:
+        run_large(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -87,8 +87,11 @@ def build(verbose=False, jobs=None):
         libdir = os.path.join(cuda, "lib64")
         if not os.path.isdir(libdir):
             libdir = os.path.join(cuda, "lib")
+        # --no-undefined: a symbol missing from the objects fails the build
+        # here, not the first dlopen on a GPU machine
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs +
-             ["-L" + libdir, "-lcusolver", "-Xlinker", "-rpath," + libdir], verbose)
+             ["-L" + libdir, "-lcusolver", "-Xlinker", "-rpath," + libdir,
+              "-Xlinker", "--no-undefined"], verbose)
     compat_src = os.path.join(CSRC, "sep_fdcompat.c")
     if os.path.exists(compat_src) and _stale(COMPAT_LIB, compat_src, deps + [LIB]):
         _run(["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-I" + os.path.join(ROOT, "include"),

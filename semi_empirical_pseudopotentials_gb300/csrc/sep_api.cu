@@ -506,6 +506,9 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
   RET(filter_device(c, c->w_start.as<double>(), ns, an_re.data(), zn.data(), ms, nc, 4.0 / dE,
                     vmin, d_psi));
   RET(normalize_device(c, d_psi, m));  // filter.c:33 per cycle
+  // ortho holds a second m x n block (its orthonormal rows) beside psi, plus
+  // about 6 GB of contraction workspace: make room on large grids
+  RET(release_filter_workspace_if_short(c, sizeof(double) * (size_t)n * m + ((size_t)6 << 30)));
   CK(cudaEventRecord(ev[2], c->stream));
   long k = 0;
   RET(ortho_device(c, d_psi, m, &k));

@@ -452,6 +452,14 @@ int rotate_rows(sep_ctx* c, double* d_psi, long long m, long long k, const doubl
 
 }  // namespace
 
+int release_filter_workspace_if_short(sep_ctx* c, size_t need) {
+  if (free_device_bytes() >= need || c->batch_holds > 0) return kOk;
+  CK(cudaStreamSynchronize(c->stream));
+  drop_graphs(c);
+  for (DevBuf* b : {&c->w_hist, &c->w_fft, &c->w_acc, &c->w_start}) b->release();
+  return kOk;
+}
+
 // =========================================================================
 int filter_device(sep_ctx* c, const double* d_start, long ns, const double* an_re,
                   const double* zn, long ms, long nc, double dE_1, double vmin,

@@ -95,6 +95,10 @@ int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nst
 int energy_all_device(sep_ctx* c, const double* d_psi, long m, double* ene_host);
 int energy_range_device(sep_ctx* c, double vmin, double* emax, double* dE, long* iters);
 int ortho_device(sep_ctx* c, double* d_psi, long m, long* mkept);
+// Frees the Newton filter's workspaces (history ring, transform and
+// accumulator grids) and the start states when fewer than `need` bytes of
+// device memory are free; the next filter call allocates them again.
+int release_filter_workspace_if_short(sep_ctx* c, size_t need);
 // keep_hpsi: also return H psi of the rotated states (rotated with them) in
 // *hpsi when the device has room for it, else *hpsi = nullptr
 int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host,

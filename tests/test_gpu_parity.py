@@ -48,7 +48,9 @@ def test_hamiltonian_matches_reference_output(golden):
 
 
 @pytest.mark.parametrize("dims", [(16, 18, 20), (36, 36, 36), (32, 40, 48), (64, 64, 64),
-                                  (56, 72, 80), (96, 112, 128), (128, 128, 128)])
+                                  (56, 72, 80), (96, 112, 128), (128, 128, 128),
+                                  (192, 160, 24), (256, 192, 16), (16, 24, 256),
+                                  (160, 16, 192)])
 def test_hamiltonian_matches_oracle(dims):
     steps, pot = _random_system(dims)
     n = int(np.prod(dims))
