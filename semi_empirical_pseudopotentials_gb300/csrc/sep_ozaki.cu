@@ -26,7 +26,10 @@ constexpr int kStages = 4;
 constexpr int kStageA = kSlices * kTileM * kChunkK * 2;    // 28672 bytes: one block
 constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 14336 bytes: half a block
 constexpr int kStageBytes = kStageA + kStageB;             // 43008 bytes
-constexpr uint32_t kRowGroupStride = kSlices * 256;        // bytes between 8-row groups
+constexpr uint32_t kRowGroupStride = 256;                  // bytes between 8-row groups
+constexpr uint32_t kSliceBytes = 16 * 256;                 // one digit of a 128-row block
+constexpr uint32_t kHalfSliceBytes = 8 * 256;              // one digit of 64 rows
+constexpr int kMaxN = 256;                                 // widest MMA (4 digits of B)
 constexpr int kTmemCols = 512;                              // kSlices * 64 = 448 used
 constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 8
 constexpr long long kSpin = 1LL << 26;                      // bounded waits
@@ -177,7 +180,7 @@ __device__ __forceinline__ uint32_t bf16_pair(int lo, int hi) {
 __device__ __forceinline__ long long plane_off(int s, long long kc, long long rb, long long nkc,
                                                long long nrb, int rr, int kk) {
   (void)nrb;
-  return (rb * nkc + kc) * kBlockElems + (((rr >> 3) * kSlices + s) * 2 + (kk >> 3)) * 64 +
+  return (rb * nkc + kc) * kBlockElems + ((s * 16 + (rr >> 3)) * 2 + (kk >> 3)) * 64 +
          (rr & 7) * 8 + (kk & 7);
 }
 
@@ -348,7 +351,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
   const uint32_t tmem = tmem_slot;
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const int half = warp >> 2;  // which 32 of the tile's 64 columns this warp drains
-  constexpr uint32_t idesc = idesc_bf16(kTileM, kTileN);
 
   // thread 0's bookkeeping: load phases consumed, commits issued per buffer
   uint32_t ph_load[kStages], n_commit[kStages];
@@ -382,10 +384,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
       const uint32_t bar = smem_u32(&bar_load[buf]);
       mbar_expect_tx(bar, kStageBytes);
       const uint16_t* sa = a.A + ((long long)tm * a.nkc + kc) * kBlockElems;
-      const uint16_t* sb =
-          a.B + ((long long)(tn >> 1) * a.nkc + kc) * kBlockElems + (tn & 1) * (kBlockElems / 2);
+      const uint16_t* sb = a.B + ((long long)(tn >> 1) * a.nkc + kc) * kBlockElems +
+                           (tn & 1) * (kHalfSliceBytes / 2);
       bulk_g2s(base, sa, kStageA, bar);
-      bulk_g2s(base + kStageA, sb, kStageB, bar);
+      // the 64 rows of each digit of B, one after the other: any run of
+      // consecutive digits is one operand of 64 rows per digit
+#pragma unroll 1
+      for (int t = 0; t < kSlices; ++t)
+        bulk_g2s(base + kStageA + t * kHalfSliceBytes, sb + t * (kSliceBytes / 2),
+                 kHalfSliceBytes, bar);
       pending[buf] = true;
     };
 
@@ -405,14 +412,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
           tc_fence_after();
           const uint32_t base = smem0 + buf * kStageBytes;
           const bool fresh = (st % kStagesPerDrain) == 0;
+          // digit s of A times digits t0..t1 of B in one MMA of N = 64 (t1 -
+          // t0 + 1): its columns are the accumulators of levels s + t0 ..
+          // s + t1, adjacent in TMEM
 #pragma unroll 1
           for (int s = 0; s < kSlices; ++s) {
-            const uint64_t da = smem_desc(base + s * 256, 128, kRowGroupStride);
+            const uint64_t da = smem_desc(base + s * kSliceBytes, 128, kRowGroupStride);
 #pragma unroll 1
-            for (int t = 0; t < kSlices - s; ++t) {
-              const uint64_t db = smem_desc(base + kStageA + t * 256, 128, kRowGroupStride);
-              mma_bf16(tmem + (uint32_t)((s + t) * kTileN), da, db, idesc,
-                       (fresh && s == 0) ? 0u : 1u);
+            for (int t0 = 0; t0 < kSlices - s; t0 += kMaxN / kTileN) {
+              const int nt = min(kMaxN / kTileN, kSlices - s - t0);
+              const uint64_t db =
+                  smem_desc(base + kStageA + t0 * kHalfSliceBytes, 128, kRowGroupStride);
+              mma_bf16(tmem + (uint32_t)((s + t0) * kTileN), da, db,
+                       idesc_bf16(kTileM, nt * kTileN), (fresh && s == 0) ? 0u : 1u);
             }
           }
           mma_commit(smem_u32(&bar_free[buf]));

@@ -41,13 +41,13 @@ constexpr int kBlockElems = kSlices * kBlockRows * kChunkK;  // 14336 bf16: all 
 
 // Pre-tiled digit planes of one operand.  Row block rb (128 rows) and K chunk
 // kc (16 values) hold all kSlices digits in one 28,672-byte block, in the
-// tensor cores' K-major no-swizzle layout with the digits interleaved: the 8x8
-// core matrix of digit s, row group i (0..15), K group j (0..1) at
-// ((i * kSlices + s) * 2 + j) * 128 bytes, row r of it at r * 16 bytes.  So a
-// block (or its first or second 64 rows) is one contiguous copy, and digit s of
-// it is a matrix with row-group stride kSlices * 256 bytes starting s * 256
-// bytes in.  Element offset (uint16) of (row rr of the block, k, digit s):
-//   (rb * nkc + kc) * 14336 + ((i * kSlices + s) * 2 + j) * 64 + r * 8 + (k % 8).
+// tensor cores' K-major no-swizzle layout, digit-major: the 8x8 core matrix of
+// digit s, row group i (0..15), K group j (0..1) at ((s * 16 + i) * 2 + j) *
+// 128 bytes, row r of it at r * 16 bytes.  So a block is one contiguous copy,
+// digit s of it a matrix with row-group stride 256 bytes starting s * 4096
+// bytes in, and the first or second 64 rows of a digit one 2048-byte piece.
+// Element offset (uint16) of (row rr of the block, k, digit s):
+//   (rb * nkc + kc) * 14336 + ((s * 16 + i) * 2 + j) * 64 + r * 8 + (k % 8).
 struct Planes {
   uint16_t* d = nullptr;  // nrb * nkc * 14336 values
   int* expo = nullptr;    // scale exponent per row (nrb * 128 entries)
