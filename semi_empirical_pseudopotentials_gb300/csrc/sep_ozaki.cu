@@ -1,15 +1,17 @@
 // sep_ozaki.cu -- exact-split FP64 contractions on the tcgen05 tensor cores
 // (see sep_ozaki.cuh for the arithmetic).
 //
-// Kernel shape (k_oz_mma): one CTA per SM, 256 threads, persistent over work
-// items (an output tile of 128 x 64 and a range of K).  Thread 0 issues the
-// bulk copies (cp.async.bulk, mbarrier transaction counts) of the pre-tiled
-// slice blocks and the tcgen05.mma instructions; the accumulators of the
-// kSlices levels live in TMEM (kSlices x 64 FP32 columns of 128 lanes); every
-// kDrainK of K the eight warps read them back with tcgen05.ld (warp w: lanes
-// 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31 of each level) and add them
-// into two int64 fixed-point registers per output element: levels 0-3 in
-// units of 2^-24 of level 0, levels 4-6 in units of 2^-48.
+// Kernel shape (k_oz_mma): two CTAs per SM, 256 threads each, persistent
+// over work items (an output tile of 128 x 32 and a range of K).  Thread 0
+// issues the bulk copies (cp.async.bulk, mbarrier transaction counts) of the
+// pre-tiled slice blocks and the tcgen05.mma instructions; the accumulators
+// of the kSlices levels live in TMEM (kSlices x 32 FP32 columns of 128
+// lanes, 256 columns allocated per CTA); every kDrainK of K the eight warps
+// read them back with tcgen05.ld (warp w: lanes 32 (w % 4) .. + 31, columns
+// 16 (w / 4) .. + 15 of each level) and add them into two int64 fixed-point
+// registers per output element: levels 0-3 in units of 2^-24 of level 0,
+// levels 4-6 in units of 2^-48.  While one CTA of an SM drains its levels,
+// the other's products keep the tensor cores busy.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -22,18 +24,20 @@ namespace oz {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kStages = 4;
+constexpr int kCtasPerSm = 2;
+constexpr int kStages = 3;
 constexpr int kStageA = kSlices * kTileM * kChunkK * 2;    // 28672 bytes: one block
-constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 14336 bytes: half a block
-constexpr int kStageBytes = kStageA + kStageB;             // 43008 bytes
+constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 7168 bytes: a quarter block
+constexpr int kStageBytes = kStageA + kStageB;             // 35840 bytes
 constexpr uint32_t kRowGroupStride = 256;                  // bytes between 8-row groups
 constexpr uint32_t kSliceBytes = 16 * 256;                 // one digit of a 128-row block
-constexpr uint32_t kHalfSliceBytes = 8 * 256;              // one digit of 64 rows
-constexpr int kMaxN = 256;                                 // widest MMA (4 digits of B)
-constexpr int kTmemCols = 512;                              // kSlices * 64 = 448 used
+constexpr uint32_t kTileSliceBytes = (kTileN / 8) * 256;   // one digit of a B tile (32 rows)
+constexpr int kTmemCols = 256;                              // kSlices * 32 = 224 used
 constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 8
 constexpr long long kSpin = 1LL << 26;                      // bounded waits
 static_assert(kSlices * kTileN <= kTmemCols, "TMEM columns");
+static_assert(kSlices * kTileN <= 256 && (kSlices * kTileN) % 16 == 0, "one MMA per digit of A");
+static_assert(kCtasPerSm * kTmemCols <= 512, "TMEM of the SM");
 static_assert((kSlices) * kDrainK * 16384LL < (1LL << 24), "exact FP32 level sums");
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -120,19 +124,15 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
       : "memory");
 }
 
-// 32 lanes x 32 columns of 32-bit TMEM words: thread t of the warp gets lane
-// (lane base + t), columns col .. col + 31
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+// 32 lanes x 16 columns of 32-bit TMEM words: thread t of the warp gets lane
+// (lane base + t), columns col .. col + 15
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
         "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-        "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
-        "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
-        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
-        "=r"(v[31])
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
       : "r"(taddr)
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -308,9 +308,9 @@ __device__ __forceinline__ void tile_of(const MmaArgs& a, int t, int& tm, int& t
     tn = t - tm * a.tiles_n;
     return;
   }
-  // tiles with a column >= a row: tn >= 2 tm
+  // tiles with a column >= a row: tn >= (kTileM / kTileN) tm
   for (tm = 0; tm < a.tiles_m; ++tm) {
-    const int first = 2 * tm;
+    const int first = (kTileM / kTileN) * tm;
     const int cnt = a.tiles_n > first ? a.tiles_n - first : 0;
     if (t < cnt) {
       tn = first + t;
@@ -321,7 +321,7 @@ __device__ __forceinline__ void tile_of(const MmaArgs& a, int t, int& tm, int& t
   tm = tn = 0;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) k_oz_mma(const MmaArgs a) {
   extern __shared__ __align__(1024) uint8_t stage_mem[];
   __shared__ __align__(8) uint64_t bar_load[kStages];
   __shared__ __align__(8) uint64_t bar_free[kStages];
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  const int half = warp >> 2;  // which 32 of the tile's 64 columns this warp drains
+  const int half = warp >> 2;  // which 16 of the tile's 32 columns this warp drains
 
   // thread 0's bookkeeping: load phases consumed, commits issued per buffer
   uint32_t ph_load[kStages], n_commit[kStages];
@@ -375,24 +375,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
     if (kc1 > a.nkc) kc1 = a.nkc;
     const int nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);  // the host leaves no split empty
 
-    long long Rh[32], Rl[32];
+    constexpr int CW = kTileN / 2;  // columns per thread
+    long long Rh[CW], Rl[CW];
 #pragma unroll
-    for (int c = 0; c < 32; ++c) Rh[c] = Rl[c] = 0;
+    for (int c = 0; c < CW; ++c) Rh[c] = Rl[c] = 0;
 
     auto issue = [&](long long kc, int buf) {
       const uint32_t base = smem0 + buf * kStageBytes;
       const uint32_t bar = smem_u32(&bar_load[buf]);
       mbar_expect_tx(bar, kStageBytes);
       const uint16_t* sa = a.A + ((long long)tm * a.nkc + kc) * kBlockElems;
-      const uint16_t* sb = a.B + ((long long)(tn >> 1) * a.nkc + kc) * kBlockElems +
-                           (tn & 1) * (kHalfSliceBytes / 2);
+      constexpr int kTilesPerBlock = kBlockRows / kTileN;
+      const uint16_t* sb = a.B + ((long long)(tn / kTilesPerBlock) * a.nkc + kc) * kBlockElems +
+                           (tn % kTilesPerBlock) * (kTileSliceBytes / 2);
       bulk_g2s(base, sa, kStageA, bar);
-      // the 64 rows of each digit of B, one after the other: any run of
-      // consecutive digits is one operand of 64 rows per digit
+      // the 32 rows of each digit of B, one after the other: any run of
+      // consecutive digits is one operand of 32 rows per digit
 #pragma unroll 1
       for (int t = 0; t < kSlices; ++t)
-        bulk_g2s(base + kStageA + t * kHalfSliceBytes, sb + t * (kSliceBytes / 2),
-                 kHalfSliceBytes, bar);
+        bulk_g2s(base + kStageA + t * kTileSliceBytes, sb + t * (kSliceBytes / 2),
+                 kTileSliceBytes, bar);
       pending[buf] = true;
     };
 
@@ -412,20 +414,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
           tc_fence_after();
           const uint32_t base = smem0 + buf * kStageBytes;
           const bool fresh = (st % kStagesPerDrain) == 0;
-          // digit s of A times digits t0..t1 of B in one MMA of N = 64 (t1 -
-          // t0 + 1): its columns are the accumulators of levels s + t0 ..
-          // s + t1, adjacent in TMEM
+          // digit s of A times digits 0 .. kSlices-1-s of B in one MMA of
+          // N = 32 (kSlices - s): its columns are the accumulators of levels
+          // s .. kSlices-1, adjacent in TMEM
+          const uint64_t db = smem_desc(base + kStageA, 128, kRowGroupStride);
 #pragma unroll 1
           for (int s = 0; s < kSlices; ++s) {
             const uint64_t da = smem_desc(base + s * kSliceBytes, 128, kRowGroupStride);
-#pragma unroll 1
-            for (int t0 = 0; t0 < kSlices - s; t0 += kMaxN / kTileN) {
-              const int nt = min(kMaxN / kTileN, kSlices - s - t0);
-              const uint64_t db =
-                  smem_desc(base + kStageA + t0 * kHalfSliceBytes, 128, kRowGroupStride);
-              mma_bf16(tmem + (uint32_t)((s + t0) * kTileN), da, db,
-                       idesc_bf16(kTileM, nt * kTileN), (fresh && s == 0) ? 0u : 1u);
-            }
+            mma_bf16(tmem + (uint32_t)(s * kTileN), da, db,
+                     idesc_bf16(kTileM, (kSlices - s) * kTileN), (fresh && s == 0) ? 0u : 1u);
           }
           mma_commit(smem_u32(&bar_free[buf]));
           n_commit[buf]++;
@@ -448,10 +445,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
         tc_fence_after();
 #pragma unroll
         for (int l = 0; l < kSlices; ++l) {
-          uint32_t v[32];
-          tmem_ld32(tmem + lane_base + (uint32_t)(l * kTileN + half * 32), v);
+          uint32_t v[CW];
+          tmem_ld16(tmem + lane_base + (uint32_t)(l * kTileN + half * CW), v);
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
+          for (int c = 0; c < CW; ++c) {
             const long long w = (long long)__float2int_rn(__uint_as_float(v[c]));
             if (l <= 3)
               Rh[c] += w << (24 - 8 * l);
@@ -471,21 +468,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_oz_mma(const MmaArgs a) {
         if (n_commit[b] > 0) ok = mbar_wait(smem_u32(&bar_free[b]), (n_commit[b] - 1) & 1, a.err, 5);
     ok = __syncthreads_and(ok);
     if (!ok) break;
-    // output row 32 (warp % 4) + lane, columns 32 half .. + 31 of tile (tm, tn)
+    // output row 32 (warp % 4) + lane, columns CW half .. + CW-1 of tile (tm, tn)
     const long long i = (long long)tm * kTileM + (warp & 3) * 32 + (tid & 31);
-    const long long j0 = (long long)tn * kTileN + half * 32;
+    const long long j0 = (long long)tn * kTileN + half * CW;
     if (a.nsplit > 1) {
       long long* dh = a.part + ((long long)split * a.prow + i) * a.pcol + j0;
       long long* dl = dh + (long long)a.nsplit * a.prow * a.pcol;
 #pragma unroll
-      for (int c = 0; c < 32; c += 2) {
+      for (int c = 0; c < CW; c += 2) {
         *reinterpret_cast<longlong2*>(dh + c) = make_longlong2(Rh[c], Rh[c + 1]);
         *reinterpret_cast<longlong2*>(dl + c) = make_longlong2(Rl[c], Rl[c + 1]);
       }
     } else if (i < a.m) {
       const int ei = a.ea[i];
 #pragma unroll
-      for (int c = 0; c < 32; ++c) {
+      for (int c = 0; c < CW; ++c) {
         const long long j = j0 + c;
         if (j < a.n && (!a.sym || j >= i)) {
           const double r = (double)Rh[c] + (double)Rl[c] * 0x1p-24;
@@ -556,7 +553,8 @@ int tile_count(long long m, long long n, bool sym) {
   const int tmc = (int)cdiv(m, kTileM), tnc = (int)cdiv(n, kTileN);
   if (!sym) return tmc * tnc;
   int t = 0;
-  for (int tm = 0; tm < tmc; ++tm) t += tnc > 2 * tm ? tnc - 2 * tm : 0;
+  constexpr int r = kTileM / kTileN;
+  for (int tm = 0; tm < tmc; ++tm) t += tnc > r * tm ? tnc - r * tm : 0;
   return t;
 }
 }  // namespace
@@ -605,7 +603,7 @@ int choose_splits(long long m, long long n, long long k, bool sym) {
   // two drain periods of K
   const long long tiles = tile_count(m, n, sym);
   const long long nkc = cdiv(k, kChunkK);
-  const long long sms = sm_count();
+  const long long sms = (long long)kCtasPerSm * sm_count();  // CTA slots
   const long long cap = std::max<long long>(1, nkc / (2 * (kDrainK / kChunkK)));
   long long best = 1;
   double best_eff = -1.0;
@@ -665,7 +663,7 @@ cudaError_t gemm_nt(const Planes& A, const Planes& B, double alpha, bool sym, bo
   a.err = err;
   const long long items = (long long)a.ntiles * a.nsplit;
   if (items < 1) return cudaSuccess;
-  const unsigned grid = (unsigned)std::min<long long>(items, sm_count());
+  const unsigned grid = (unsigned)std::min<long long>(items, (long long)kCtasPerSm * sm_count());
   k_oz_mma<<<grid, kThreads, kStages * kStageBytes, s>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess || a.nsplit == 1) return e;

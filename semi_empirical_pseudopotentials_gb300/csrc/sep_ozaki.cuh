@@ -33,7 +33,7 @@ namespace oz {
 
 constexpr int kSlices = 7;          // digits per value (55 bits)
 constexpr int kTileM = 128;         // rows of A per tile (TMEM lanes)
-constexpr int kTileN = 64;          // rows of B per tile (TMEM columns per level)
+constexpr int kTileN = 32;          // rows of B per tile (TMEM columns per level)
 constexpr int kChunkK = 16;         // K per pipeline stage (one MMA per digit pair)
 constexpr int kBlockRows = 128;     // rows per pre-tiled block in global memory
 constexpr int kDrainK = 128;        // K accumulated per level before a drain
@@ -45,7 +45,7 @@ constexpr int kBlockElems = kSlices * kBlockRows * kChunkK;  // 14336 bf16: all 
 // digit s, row group i (0..15), K group j (0..1) at ((s * 16 + i) * 2 + j) *
 // 128 bytes, row r of it at r * 16 bytes.  So a block is one contiguous copy,
 // digit s of it a matrix with row-group stride 256 bytes starting s * 4096
-// bytes in, and the first or second 64 rows of a digit one 2048-byte piece.
+// bytes in, and each 32 rows of a digit one 1024-byte piece.
 // Element offset (uint16) of (row rr of the block, k, digit s):
 //   (rb * nkc + kc) * 14336 + ((s * 16 + i) * 2 + j) * 64 + r * 8 + (k % 8).
 struct Planes {
