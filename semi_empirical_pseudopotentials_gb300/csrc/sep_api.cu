@@ -145,6 +145,8 @@ sep_ctx::~sep_ctx() {
                     &w_ozA, &w_ozB, &w_ozP, &w_ozE})
     b->release();
   if (solver) cusolverDnDestroy(solver);
+  if (h2d) cudaStreamDestroy(h2d);
+  if (d2h) cudaStreamDestroy(d2h);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -415,14 +417,11 @@ int sep_filter(sep_ctx* c, const double* start, long ns, const double* an_re, co
   RET(check_ctx(c));
   if (!start || !an_re || !zn || !out || ns < 1 || ms < 1)
     return arg_fail("sep_filter: bad argument");
-  RET(to_device(c, c->w_start, start, (size_t)c->n * ns));
+  RET(ensure_buf(c, c->w_start, sizeof(double) * (size_t)c->n * ns));
   RET(ensure_buf(c, c->w_out, sizeof(double) * (size_t)c->n * ns * ms));
-  RET(filter_device(c, c->w_start.as<double>(), ns, an_re, zn, ms, nc, dE_1, vmin,
-                    c->w_out.as<double>()));
-  CK(cudaMemcpyAsync(out, c->w_out.p, sizeof(double) * (size_t)c->n * ns * ms,
-                     cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  return kOk;
+  const HostIO host{start, out};
+  return filter_device(c, c->w_start.as<double>(), ns, an_re, zn, ms, nc, dE_1, vmin,
+                       c->w_out.as<double>(), &host);
 }
 
 // ---- norms and energies --------------------------------------------------

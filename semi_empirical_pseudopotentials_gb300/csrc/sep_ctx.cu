@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "sep_ctx.cuh"
@@ -214,7 +215,8 @@ int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int 
 
 template <typename T>
 int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
-                const double* zn, long ms, long nc, double dE_1, double vmin, double* d_out) {
+                const double* zn, long ms, long nc, double dE_1, double vmin, double* d_out,
+                const HostIO* host) {
   const long long n = c->n;
   int K = c->block_steps;
   if (K > nc) K = (int)nc;
@@ -253,10 +255,53 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     CK(xy_prepare(c->g32));
     c->xy_ready = true;
   }
-  for (long long b0 = 0; b0 < B; b0 += Bc) {
-    const int bc = (int)std::min<long long>(Bc, B - b0);
-    const long long s0 = 2 * b0;
-    const long long nst = std::min<long long>(2LL * bc, ns - s0);
+  // chunks of pairs [first, first + count): at most Bc each; with host
+  // buffers the last chunk is small (8 pairs, or half of them), so that only
+  // its output copy is not under a filter (8 pairs filter at 0.94 of the rate
+  // of 32)
+  std::vector<std::pair<long long, long long>> chunks;
+  for (long long b0 = 0; b0 < B; b0 += Bc) chunks.push_back({b0, std::min<long long>(Bc, B - b0)});
+  if (host) {
+    const long long tail = std::min<long long>(8, B / 2);
+    auto& last = chunks.back();
+    if (tail > 0 && last.second > tail) {
+      last.second -= tail;
+      chunks.push_back({last.first + last.second, tail});
+    }
+  }
+  const long long nchunks = (long long)chunks.size();
+  std::vector<cudaEvent_t> ev;  // per chunk: start states up, output computed
+  if (host) {
+    for (cudaStream_t* st : {&c->h2d, &c->d2h})
+      if (!*st) CK(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    ev.assign(2 * nchunks, nullptr);
+    for (auto& e : ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  auto chunk_states = [&](long long k, long long& s0, long long& nst) {
+    s0 = 2 * chunks[k].first;
+    nst = std::min<long long>(2 * chunks[k].second, ns - s0);
+  };
+  auto upload = [&](long long k, cudaStream_t st) -> int {
+    long long s0, nst;
+    chunk_states(k, s0, nst);
+    CK(cudaMemcpyAsync(const_cast<double*>(d_start) + s0 * n, host->start + s0 * n,
+                       sizeof(double) * (size_t)(nst * n), cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(ev[2 * k], st));
+    return kOk;
+  };
+  int rc = kOk;
+  if (host) rc = upload(0, c->stream);
+  for (long long k = 0; k < nchunks && rc == kOk; ++k) {
+    const int bc = (int)chunks[k].second;
+    long long s0, nst;
+    chunk_states(k, s0, nst);
+    if (host) {
+      if (k + 1 < nchunks && (rc = upload(k + 1, c->h2d)) != kOk) break;
+      if (cudaStreamWaitEvent(c->stream, ev[2 * k], 0) != cudaSuccess) {
+        rc = cuda_fail(cudaGetLastError(), "cudaStreamWaitEvent", __LINE__);
+        break;
+      }
+    }
     CK(pack_pairs<T, double>(d_start + s0 * n, nst, n, c->w_hist.as<cx<T>>(), c->stream));
     if (c->use_graphs) {
       const long long key[8] = {bc, nst, ms, nc, K, (long long)(size_t)c->w_hist.p,
@@ -290,8 +335,25 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     }
     double* dst = d_out + s0 * ms * n;
     CK(unpack_accumulators<T>(c->w_acc.as<T>(), bc, n, (int)ms, nst, dst, c->stream));
+    if (host) {  // the chunk's output goes down while the next chunk is filtered
+      CK(cudaEventRecord(ev[2 * k + 1], c->stream));
+      CK(cudaStreamWaitEvent(c->d2h, ev[2 * k + 1], 0));
+      CK(cudaMemcpyAsync(host->out + s0 * ms * n, dst, sizeof(double) * (size_t)(nst * ms * n),
+                         cudaMemcpyDeviceToHost, c->d2h));
+    }
   }
-  return kOk;
+  if (host) {
+    cudaError_t e1 = cudaStreamSynchronize(c->h2d);
+    cudaError_t e2 = cudaStreamSynchronize(c->d2h);
+    cudaError_t e3 = cudaStreamSynchronize(c->stream);
+    for (auto e : ev) cudaEventDestroy(e);
+    if (rc == kOk) {
+      CK(e1);
+      CK(e2);
+      CK(e3);
+    }
+  }
+  return rc;
 }
 
 // complex states through H in chunks that fit the scratch
@@ -463,11 +525,11 @@ int release_filter_workspace_if_short(sep_ctx* c, size_t need) {
 // =========================================================================
 int filter_device(sep_ctx* c, const double* d_start, long ns, const double* an_re,
                   const double* zn, long ms, long nc, double dE_1, double vmin,
-                  double* d_out) {
+                  double* d_out, const HostIO* host) {
   if (ns < 1 || ms < 1 || nc < 1 || ms > 32) return arg_fail("filter: need ns, nc >= 1 and 1 <= ms <= 32");
   if (c->precision == 1)
-    return filter_impl<float>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out);
-  return filter_impl<double>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out);
+    return filter_impl<float>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out, host);
+  return filter_impl<double>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out, host);
 }
 
 int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nstates) {

@@ -63,6 +63,7 @@ struct sep_batch {
 struct sep_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t h2d = nullptr, d2h = nullptr;  // host copies beside the filter (sep_filter)
   cusolverDnHandle_t solver = nullptr;
   int precision = 0;
   long nx = 0, ny = 0, nz = 0;
@@ -88,9 +89,18 @@ struct sep_ctx {
 
 namespace sep {
 
+// Host buffers of a filter call.  With them the filter runs in chunks of
+// pairs: the start states of a chunk go up on ctx->h2d, and its output comes
+// down on ctx->d2h while the next chunk is filtered.
+struct HostIO {
+  const double* start;  // ns x n
+  double* out;          // ns x ms x n
+};
+
 // device-side operations used by the ABI (all on ctx->stream)
 int filter_device(sep_ctx* c, const double* d_start, long ns, const double* an_re,
-                  const double* zn, long ms, long nc, double dE_1, double vmin, double* d_out);
+                  const double* zn, long ms, long nc, double dE_1, double vmin, double* d_out,
+                  const HostIO* host = nullptr);
 int hamiltonian_device(sep_ctx* c, const double* d_psi, double* d_hpsi, long nstates);
 int energy_all_device(sep_ctx* c, const double* d_psi, long m, double* ene_host);
 int energy_range_device(sep_ctx* c, double vmin, double* emax, double* dE, long* iters);

@@ -1,17 +1,21 @@
 // sep_ozaki.cu -- exact-split FP64 contractions on the tcgen05 tensor cores
 // (see sep_ozaki.cuh for the arithmetic).
 //
-// Kernel shape (k_oz_mma): two CTAs per SM, 256 threads each, persistent
-// over work items (an output tile of 128 x 32 and a range of K).  Thread 0
-// issues the bulk copies (cp.async.bulk, mbarrier transaction counts) of the
-// pre-tiled slice blocks and the tcgen05.mma instructions; the accumulators
-// of the kSlices levels live in TMEM (kSlices x 32 FP32 columns of 128
-// lanes, 256 columns allocated per CTA); every kDrainK of K the eight warps
-// read them back with tcgen05.ld (warp w: lanes 32 (w % 4) .. + 31, columns
-// 16 (w / 4) .. + 15 of each level) and add them into two int64 fixed-point
-// registers per output element: levels 0-3 in units of 2^-24 of level 0,
-// levels 4-6 in units of 2^-48.  While one CTA of an SM drains its levels,
-// the other's products keep the tensor cores busy.
+// Kernel shape (k_oz_mma): one CTA per SM, persistent over work items (an
+// output tile of 128 x 64 and a range of K), nine warps with fixed roles:
+//  * warp 17, one thread: the bulk copies (cp.async.bulk, mbarrier
+//    transaction counts) of the pre-tiled slice blocks, kStages stages ahead.
+//  * warp 16, one thread: the tcgen05.mma instructions.
+//  * warps 0-7 and 8-15: the drains of the tile's two 32-column halves
+//    ("sets").  The kSlices level accumulators of a set live in TMEM (kSlices
+//    x 32 FP32 columns of 128 lanes; set c at columns 256 c).  Every kDrainK
+//    of K a set's eight warps read them back with tcgen05.ld (warp w: lanes
+//    32 (w % 4) .. + 31, 16 of the set's columns) and add them into two int64
+//    fixed-point registers per output element: levels 0-3 in units of 2^-24
+//    of level 0, levels 4-6 in units of 2^-48.
+// The two sets drain kDrainK / 2 of K apart; while one set is drained the MMA
+// thread keeps issuing the other set's products, up to kStages stages ahead,
+// so the tensor cores do not wait for the drains.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,21 +27,25 @@ namespace sep {
 namespace oz {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kCtasPerSm = 2;
-constexpr int kStages = 3;
+constexpr int kSets = 2;                                   // 32-column halves of a tile
+constexpr int kSetN = kTileN / kSets;                      // 32
+constexpr int kDrainWarps = 8 * kSets;                     // warps 0..15
+constexpr int kDrainCols = kSetN / 2;                      // columns per drain thread
+constexpr int kMmaWarp = kDrainWarps, kLoadWarp = kDrainWarps + 1;
+constexpr int kThreads = 32 * (kDrainWarps + 2);           // + the MMA and copy warps
+constexpr int kStages = 4;
 constexpr int kStageA = kSlices * kTileM * kChunkK * 2;    // 28672 bytes: one block
-constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 7168 bytes: a quarter block
-constexpr int kStageBytes = kStageA + kStageB;             // 35840 bytes
+constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 14336 bytes: 64 rows
+constexpr int kStageBytes = kStageA + kStageB;             // 43008 bytes
 constexpr uint32_t kRowGroupStride = 256;                  // bytes between 8-row groups
 constexpr uint32_t kSliceBytes = 16 * 256;                 // one digit of a 128-row block
-constexpr uint32_t kTileSliceBytes = (kTileN / 8) * 256;   // one digit of a B tile (32 rows)
-constexpr int kTmemCols = 256;                              // kSlices * 32 = 224 used
+constexpr uint32_t kSetSliceBytes = (kSetN / 8) * 256;     // one digit of a set's 32 rows
+constexpr int kTmemCols = 512;                              // set c: 256 c .. + 7 * 32
+constexpr int kSetCols = 256;
 constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 8
 constexpr long long kSpin = 1LL << 26;                      // bounded waits
-static_assert(kSlices * kTileN <= kTmemCols, "TMEM columns");
-static_assert(kSlices * kTileN <= 256 && (kSlices * kTileN) % 16 == 0, "one MMA per digit of A");
-static_assert(kCtasPerSm * kTmemCols <= 512, "TMEM of the SM");
+static_assert(kSlices * kSetN <= kSetCols && kSets * kSetCols <= kTmemCols, "TMEM columns");
+static_assert((kSlices * kSetN) % 16 == 0, "one MMA per digit of A and set");
 static_assert((kSlices) * kDrainK * 16384LL < (1LL << 24), "exact FP32 level sums");
 
 // ---- PTX wrappers ----------------------------------------------------------
@@ -136,6 +144,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
       : "r"(taddr)
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // ---- splitting -------------------------------------------------------------
@@ -321,11 +333,29 @@ __device__ __forceinline__ void tile_of(const MmaArgs& a, int t, int& tm, int& t
   tm = tn = 0;
 }
 
-__global__ void __launch_bounds__(kThreads, kCtasPerSm) k_oz_mma(const MmaArgs a) {
+// set c's level accumulators are drained after local stage st of an item
+__device__ __forceinline__ bool drain_after(int c, int st, int nst) {
+  return st == nst - 1 || ((st + (kStagesPerDrain / 2) * c) % kStagesPerDrain) ==
+                              kStagesPerDrain - 1;
+}
+
+__device__ __forceinline__ void item_of(const MmaArgs& a, int item, int& split, int& tm, int& tn,
+                                        long long& kc0, int& nst) {
+  // split-major order: CTAs running together share K ranges (and L2 lines)
+  split = item / a.ntiles;
+  tile_of(a, item - split * a.ntiles, tm, tn);
+  kc0 = split * a.kc_per_split;
+  long long kc1 = kc0 + a.kc_per_split;
+  if (kc1 > a.nkc) kc1 = a.nkc;
+  nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);  // the host leaves no split empty
+}
+
+__global__ void __maxnreg__(96) k_oz_mma(const MmaArgs a) {
   extern __shared__ __align__(1024) uint8_t stage_mem[];
-  __shared__ __align__(8) uint64_t bar_load[kStages];
-  __shared__ __align__(8) uint64_t bar_free[kStages];
-  __shared__ __align__(8) uint64_t bar_drain;
+  __shared__ __align__(8) uint64_t bar_load[kStages];   // copies of a stage landed
+  __shared__ __align__(8) uint64_t bar_free[kStages];   // both sets' products of a stage done
+  __shared__ __align__(8) uint64_t bar_full[kSets];     // a set's period of products done
+  __shared__ __align__(8) uint64_t bar_drained[kSets];  // a set's accumulators read back
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t smem0 = smem_u32(stage_mem);
@@ -333,9 +363,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) k_oz_mma(const MmaArgs a
   if (tid == 0) {
     for (int b = 0; b < kStages; ++b) {
       mbar_init(smem_u32(&bar_load[b]), 1);
-      mbar_init(smem_u32(&bar_free[b]), 1);
+      mbar_init(smem_u32(&bar_free[b]), kSets);
     }
-    mbar_init(smem_u32(&bar_drain), 1);
+    for (int c = 0; c < kSets; ++c) {
+      mbar_init(smem_u32(&bar_full[c]), 1);
+      mbar_init(smem_u32(&bar_drained[c]), 32 * kDrainWarps / kSets);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -349,154 +382,192 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) k_oz_mma(const MmaArgs a
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  const int half = warp >> 2;  // which 16 of the tile's 32 columns this warp drains
-
-  // thread 0's bookkeeping: load phases consumed, commits issued per buffer
-  uint32_t ph_load[kStages], n_commit[kStages];
-  bool pending[kStages];
-  for (int b = 0; b < kStages; ++b) {
-    ph_load[b] = 0;
-    n_commit[b] = 0;
-    pending[b] = false;
-  }
-  uint32_t ph_drain = 0;
-  bool ok = true;
   const int items = a.ntiles * a.nsplit;
-  long long gstage = 0;  // stages consumed by this CTA so far (buffer = gstage % kStages)
+  bool ok = true;
 
-  for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
-    // split-major order: CTAs running together share K ranges (and L2 lines)
-    const int split = item / a.ntiles, tile = item - split * a.ntiles;
-    int tm, tn;
-    tile_of(a, tile, tm, tn);
-    const long long kc0 = split * a.kc_per_split;
-    long long kc1 = kc0 + a.kc_per_split;
-    if (kc1 > a.nkc) kc1 = a.nkc;
-    const int nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);  // the host leaves no split empty
-
-    constexpr int CW = kTileN / 2;  // columns per thread
-    long long Rh[CW], Rl[CW];
-#pragma unroll
-    for (int c = 0; c < CW; ++c) Rh[c] = Rl[c] = 0;
-
-    auto issue = [&](long long kc, int buf) {
-      const uint32_t base = smem0 + buf * kStageBytes;
-      const uint32_t bar = smem_u32(&bar_load[buf]);
-      mbar_expect_tx(bar, kStageBytes);
-      const uint16_t* sa = a.A + ((long long)tm * a.nkc + kc) * kBlockElems;
-      constexpr int kTilesPerBlock = kBlockRows / kTileN;
-      const uint16_t* sb = a.B + ((long long)(tn / kTilesPerBlock) * a.nkc + kc) * kBlockElems +
-                           (tn % kTilesPerBlock) * (kTileSliceBytes / 2);
-      bulk_g2s(base, sa, kStageA, bar);
-      // the 32 rows of each digit of B, one after the other: any run of
-      // consecutive digits is one operand of 32 rows per digit
+  if (warp == kLoadWarp) {
+    // ---------------- copies ----------------
+    if ((tid & 31) == 0) {
+      long long gs = 0;  // global stage
+      for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+        int split, tm, tn, nst;
+        long long kc0;
+        item_of(a, item, split, tm, tn, kc0, nst);
+        const uint16_t* ablk = a.A + (long long)tm * a.nkc * kBlockElems;
+        const uint16_t* bblk = a.B + (long long)(tn >> 1) * a.nkc * kBlockElems +
+                               (tn & 1) * kSets * (kSetSliceBytes / 2);
+        for (int st = 0; st < nst && ok; ++st, ++gs) {
+          const int b = (int)(gs % kStages);
+          // the buffer's previous stage: both sets' products done
+          if (gs >= kStages)
+            ok = mbar_wait(smem_u32(&bar_free[b]), (uint32_t)((gs / kStages - 1) & 1), a.err, 2);
+          if (!ok) break;
+          const uint32_t base = smem0 + b * kStageBytes, bar = smem_u32(&bar_load[b]);
+          const long long kc = kc0 + st;
+          mbar_expect_tx(bar, kStageBytes);
+          bulk_g2s(base, ablk + kc * kBlockElems, kStageA, bar);
+          // set c's 32 rows of every digit, digits consecutive: any run of
+          // digits of one set is one operand of 32 rows per digit
 #pragma unroll 1
-      for (int t = 0; t < kSlices; ++t)
-        bulk_g2s(base + kStageA + t * kTileSliceBytes, sb + t * (kSliceBytes / 2),
-                 kTileSliceBytes, bar);
-      pending[buf] = true;
-    };
-
-    // prologue: every buffer is free (the previous item ended with a drain,
-    // which waited for all of its tensor-core work)
-    if (tid == 0)
-      for (int j = 0; j < kStages && j < nst; ++j) issue(kc0 + j, (int)((gstage + j) % kStages));
-
-    for (int st = 0; st < nst; ++st) {
-      const int buf = (int)((gstage + st) % kStages);
-      const bool drain_now = (st % kStagesPerDrain) == kStagesPerDrain - 1 || st == nst - 1;
-      if (tid == 0 && ok) {
-        ok = mbar_wait(smem_u32(&bar_load[buf]), ph_load[buf], a.err, 1);
-        if (ok) {
-          ph_load[buf] ^= 1;
-          pending[buf] = false;
-          tc_fence_after();
-          const uint32_t base = smem0 + buf * kStageBytes;
-          const bool fresh = (st % kStagesPerDrain) == 0;
-          // digit s of A times digits 0 .. kSlices-1-s of B in one MMA of
-          // N = 32 (kSlices - s): its columns are the accumulators of levels
-          // s .. kSlices-1, adjacent in TMEM
-          const uint64_t db = smem_desc(base + kStageA, 128, kRowGroupStride);
+          for (int c = 0; c < kSets; ++c)
 #pragma unroll 1
-          for (int s = 0; s < kSlices; ++s) {
-            const uint64_t da = smem_desc(base + s * kSliceBytes, 128, kRowGroupStride);
-            mma_bf16(tmem + (uint32_t)(s * kTileN), da, db,
-                     idesc_bf16(kTileM, (kSlices - s) * kTileN), (fresh && s == 0) ? 0u : 1u);
-          }
-          mma_commit(smem_u32(&bar_free[buf]));
-          n_commit[buf]++;
-          if (drain_now) mma_commit(smem_u32(&bar_drain));
-          // refill the buffer of the previous stage once its products are done
-          if (st >= 1 && st - 1 + kStages < nst) {
-            const int pb = (int)((gstage + st - 1) % kStages);
-            ok = mbar_wait(smem_u32(&bar_free[pb]), (n_commit[pb] - 1) & 1, a.err, 2);
-            if (ok) issue(kc0 + st - 1 + kStages, pb);
-          }
+            for (int t = 0; t < kSlices; ++t)
+              bulk_g2s(base + kStageA + (c * kSlices + t) * kSetSliceBytes,
+                       bblk + kc * kBlockElems + t * (kSliceBytes / 2) + c * (kSetSliceBytes / 2),
+                       kSetSliceBytes, bar);
         }
       }
-      if (drain_now) {
-        ok = __syncthreads_and(ok);
+      // the last copies of every buffer land before the shared memory is released
+      for (long long g = (gs > kStages ? gs - kStages : 0); g < gs; ++g)
+        mbar_wait(smem_u32(&bar_load[g % kStages]), (uint32_t)((g / kStages) & 1), a.err, 4);
+    }
+  } else if (warp == kMmaWarp) {
+    // ---------------- products ----------------
+    if ((tid & 31) == 0) {
+      long long g0 = 0;         // global stage index of the item's first stage
+      long long seen = -1;      // last global stage whose copies were seen landed
+      uint32_t f0 = 0, f1 = 0;  // periods ended (bar_full commits) per set
+      uint32_t d0 = 0, d1 = 0;  // drains seen complete per set
+      for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+        int split, tm, tn, nst;
+        long long kc0;
+        item_of(a, item, split, tm, tn, kc0, nst);
+        int n0 = 0, n1 = 0;  // next local stage per set
+        while (ok && (n0 < nst || n1 < nst)) {
+          // a set may run at most kStages - 1 stages ahead of the other: the
+          // copies of a stage wait for the buffer's previous stage
+          const int lo = min(n0, n1);
+          // the set that is behind first; a set whose new period needs its
+          // accumulators drained waits, and the other set goes on
+          bool done_one = false;
+          for (int pass = 0; pass < 2 && ok && !done_one; ++pass) {
+            const int c = ((n0 <= n1) ? 0 : 1) ^ pass;
+            int& nx = c ? n1 : n0;
+            uint32_t& nf = c ? f1 : f0;
+            uint32_t& nd = c ? d1 : d0;
+            const int st = nx;
+            if (st >= nst || st >= lo + kStages) continue;
+            const bool fresh = st == 0 || drain_after(c, st - 1, nst);
+            if (fresh && nd < nf) {
+              if (!mbar_try(smem_u32(&bar_drained[c]), nd & 1)) continue;
+              ++nd;
+              if (nd < nf) continue;
+            }
+            const long long gs = g0 + st;
+            const int b = (int)(gs % kStages);
+            if (gs > seen) {  // the first set to reach a stage waits for its copies
+              ok = mbar_wait(smem_u32(&bar_load[b]), (uint32_t)((gs / kStages) & 1), a.err, 1);
+              if (!ok) break;
+              seen = gs;
+            }
+            tc_fence_after();
+            const uint32_t base = smem0 + b * kStageBytes;
+            const uint64_t db =
+                smem_desc(base + kStageA + c * kSlices * kSetSliceBytes, 128, kRowGroupStride);
+            // digit s of A times digits 0 .. kSlices-1-s of B: the
+            // accumulators of levels s .. kSlices-1, adjacent in TMEM
+#pragma unroll 1
+            for (int s = 0; s < kSlices; ++s) {
+              const uint64_t da = smem_desc(base + s * kSliceBytes, 128, kRowGroupStride);
+              mma_bf16(tmem + (uint32_t)(c * kSetCols + s * kSetN), da, db,
+                       idesc_bf16(kTileM, (kSlices - s) * kSetN), (fresh && s == 0) ? 0u : 1u);
+            }
+            mma_commit(smem_u32(&bar_free[b]));
+            if (drain_after(c, st, nst)) {
+              mma_commit(smem_u32(&bar_full[c]));
+              ++nf;
+            }
+            ++nx;
+            done_one = true;
+          }
+          if (ok && !done_one) {
+            // both sets wait for a drain: block on the set that is behind
+            int c = (n0 <= n1) ? 0 : 1;
+            if ((c ? n1 : n0) >= nst) c ^= 1;
+            uint32_t& nf = c ? f1 : f0;
+            uint32_t& nd = c ? d1 : d0;
+            if (nd < nf) {
+              ok = mbar_wait(smem_u32(&bar_drained[c]), nd & 1, a.err, 3);
+              if (ok) ++nd;
+            } else {  // nothing to wait for and nothing issued: a logic error
+              atomicCAS(a.err, 0, 7);
+              ok = false;
+            }
+          }
+        }
+        g0 += nst;
+      }
+      // the last drains of both sets before the accumulators are released
+      while (ok && d0 < f0) {
+        ok = mbar_wait(smem_u32(&bar_drained[0]), d0 & 1, a.err, 5);
+        if (ok) ++d0;
+      }
+      while (ok && d1 < f1) {
+        ok = mbar_wait(smem_u32(&bar_drained[1]), d1 & 1, a.err, 5);
+        if (ok) ++d1;
+      }
+    }
+  } else {
+    // ---- drains: set c = warp / 8, lanes 32 (warp % 4) .. + 31, columns
+    // kDrainCols h .. + kDrainCols-1 of the set, h = (warp / 4) % 2 ----
+    const int c = warp / 8, h = (warp / 4) & 1;
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    uint32_t nfull_seen = 0;
+    for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
+      int split, tm, tn, nst;
+      long long kc0;
+      item_of(a, item, split, tm, tn, kc0, nst);
+      long long Rh[kDrainCols], Rl[kDrainCols];
+#pragma unroll
+      for (int j = 0; j < kDrainCols; ++j) Rh[j] = Rl[j] = 0;
+      for (int st = 0; st < nst && ok; ++st) {
+        if (!drain_after(c, st, nst)) continue;
+        ok = mbar_wait(smem_u32(&bar_full[c]), nfull_seen & 1, a.err, 6);
         if (!ok) break;
-        ok = mbar_wait(smem_u32(&bar_drain), ph_drain, a.err, 3);
-        ok = __syncthreads_and(ok);
-        if (!ok) break;
-        ph_drain ^= 1;
+        ++nfull_seen;
         tc_fence_after();
 #pragma unroll
         for (int l = 0; l < kSlices; ++l) {
-          uint32_t v[CW];
-          tmem_ld16(tmem + lane_base + (uint32_t)(l * kTileN + half * CW), v);
+          uint32_t v[kDrainCols];
+          tmem_ld16(tmem + lane_base + (uint32_t)(c * kSetCols + l * kSetN + h * kDrainCols), v);
 #pragma unroll
-          for (int c = 0; c < CW; ++c) {
-            const long long w = (long long)__float2int_rn(__uint_as_float(v[c]));
+          for (int j = 0; j < kDrainCols; ++j) {
+            const long long w = (long long)__float2int_rn(__uint_as_float(v[j]));
             if (l <= 3)
-              Rh[c] += w << (24 - 8 * l);
+              Rh[j] += w << (24 - 8 * l);
             else
-              Rl[c] += w << (48 - 8 * l);
+              Rl[j] += w << (48 - 8 * l);
           }
         }
         tc_fence_before();
-        __syncthreads();
+        mbar_arrive(smem_u32(&bar_drained[c]));
       }
-    }
-    gstage += nst;
-    if (!ok) break;
-    // consume the last commit of every buffer (all complete after the drain)
-    if (tid == 0)
-      for (int b = 0; b < kStages && ok; ++b)
-        if (n_commit[b] > 0) ok = mbar_wait(smem_u32(&bar_free[b]), (n_commit[b] - 1) & 1, a.err, 5);
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    // output row 32 (warp % 4) + lane, columns CW half .. + CW-1 of tile (tm, tn)
-    const long long i = (long long)tm * kTileM + (warp & 3) * 32 + (tid & 31);
-    const long long j0 = (long long)tn * kTileN + half * CW;
-    if (a.nsplit > 1) {
-      long long* dh = a.part + ((long long)split * a.prow + i) * a.pcol + j0;
-      long long* dl = dh + (long long)a.nsplit * a.prow * a.pcol;
+      if (!ok) break;
+      // output row 32 (warp % 4) + lane, columns 32 c + 16 h .. + 15 of tile (tm, tn)
+      const long long i = (long long)tm * kTileM + (warp & 3) * 32 + (tid & 31);
+      const long long j0 = (long long)tn * kTileN + c * kSetN + h * kDrainCols;
+      if (a.nsplit > 1) {
+        long long* dh = a.part + ((long long)split * a.prow + i) * a.pcol + j0;
+        long long* dl = dh + (long long)a.nsplit * a.prow * a.pcol;
 #pragma unroll
-      for (int c = 0; c < CW; c += 2) {
-        *reinterpret_cast<longlong2*>(dh + c) = make_longlong2(Rh[c], Rh[c + 1]);
-        *reinterpret_cast<longlong2*>(dl + c) = make_longlong2(Rl[c], Rl[c + 1]);
-      }
-    } else if (i < a.m) {
-      const int ei = a.ea[i];
+        for (int j = 0; j < kDrainCols; j += 2) {
+          *reinterpret_cast<longlong2*>(dh + j) = make_longlong2(Rh[j], Rh[j + 1]);
+          *reinterpret_cast<longlong2*>(dl + j) = make_longlong2(Rl[j], Rl[j + 1]);
+        }
+      } else if (i < a.m) {
+        const int ei = a.ea[i];
 #pragma unroll
-      for (int c = 0; c < CW; ++c) {
-        const long long j = j0 + c;
-        if (j < a.n && (!a.sym || j >= i)) {
-          const double r = (double)Rh[c] + (double)Rl[c] * 0x1p-24;
-          const double v = scale2(a.alpha * r, ei + a.eb[j] - 38);
-          a.C[i * a.ldc + j] = a.acc ? a.C[i * a.ldc + j] + v : v;
-          if (a.sym && j > i) a.C[j * a.ldc + i] = a.acc ? a.C[j * a.ldc + i] + v : v;
+        for (int jj = 0; jj < kDrainCols; ++jj) {
+          const long long j = j0 + jj;
+          if (j < a.n && (!a.sym || j >= i)) {
+            const double r = (double)Rh[jj] + (double)Rl[jj] * 0x1p-24;
+            const double v = scale2(a.alpha * r, ei + a.eb[j] - 38);
+            a.C[i * a.ldc + j] = a.acc ? a.C[i * a.ldc + j] + v : v;
+            if (a.sym && j > i) a.C[j * a.ldc + i] = a.acc ? a.C[j * a.ldc + i] + v : v;
+          }
         }
       }
     }
-  }
-  if (!ok && tid == 0) {
-    // let copies still in flight land before the shared memory is released
-    for (int b = 0; b < kStages; ++b)
-      if (pending[b]) mbar_wait(smem_u32(&bar_load[b]), ph_load[b], a.err, 4);
   }
   tc_fence_before();
   __syncthreads();
@@ -603,7 +674,7 @@ int choose_splits(long long m, long long n, long long k, bool sym) {
   // two drain periods of K
   const long long tiles = tile_count(m, n, sym);
   const long long nkc = cdiv(k, kChunkK);
-  const long long sms = (long long)kCtasPerSm * sm_count();  // CTA slots
+  const long long sms = sm_count();
   const long long cap = std::max<long long>(1, nkc / (2 * (kDrainK / kChunkK)));
   long long best = 1;
   double best_eff = -1.0;
@@ -663,7 +734,7 @@ cudaError_t gemm_nt(const Planes& A, const Planes& B, double alpha, bool sym, bo
   a.err = err;
   const long long items = (long long)a.ntiles * a.nsplit;
   if (items < 1) return cudaSuccess;
-  const unsigned grid = (unsigned)std::min<long long>(items, (long long)kCtasPerSm * sm_count());
+  const unsigned grid = (unsigned)std::min<long long>(items, sm_count());
   k_oz_mma<<<grid, kThreads, kStages * kStageBytes, s>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess || a.nsplit == 1) return e;

@@ -33,7 +33,7 @@ namespace oz {
 
 constexpr int kSlices = 7;          // digits per value (55 bits)
 constexpr int kTileM = 128;         // rows of A per tile (TMEM lanes)
-constexpr int kTileN = 32;          // rows of B per tile (TMEM columns per level)
+constexpr int kTileN = 64;          // rows of B per tile (two sets of 32 TMEM columns per level)
 constexpr int kChunkK = 16;         // K per pipeline stage (one MMA per digit pair)
 constexpr int kBlockRows = 128;     // rows per pre-tiled block in global memory
 constexpr int kDrainK = 128;        // K accumulated per level before a drain
