@@ -200,37 +200,32 @@ __device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs
                                               long long off, long long goff, float alpha,
                                               float beta) {
   using S = XyShape<L>;
-  constexpr int NCH = 4;  // the epilogue in chunks of N2 / 4 elements
-  static_assert(S::n2 % NCH == 0, "epilogue chunks");
-  constexpr int HN = S::n2 / NCH;
   const C* __restrict__ pin = a.psi_in ? a.psi_in + off : nullptr;
   const float* __restrict__ pv = a.pot + goff;
   C* __restrict__ pout = a.psi_out + off;
   for (int i = threadIdx.x; i < L * 8; i += S::nt) {
     const int n1 = i & 7, row = row_of_group(i >> 3);
     const long long g0 = (long long)row * L + n1;
+    // the item's psi_{j-1} and V are requested before its transform, so
+    // their latency runs under the shared-memory reads and the DFT
+    C q[S::n2];
+    float v[S::n2];
+#pragma unroll
+    for (int n2 = 0; n2 < S::n2; ++n2) {
+      const long long e = g0 + S::n1 * n2;
+      q[n2] = pin ? pin[e] : mk<float>(0.f, 0.f);
+      v[n2] = pv[e];
+    }
     C* p = pl + row * S::rs + n1;
     C u[S::n2];
 #pragma unroll
     for (int k2 = 0; k2 < S::n2; ++k2) u[k2] = p[S::n1 * k2];
     Dft<S::n2, +1, float>::run(u);
 #pragma unroll
-    for (int h = 0; h < NCH; ++h) {
-      C q[HN];
-      float v[HN];
-#pragma unroll
-      for (int m = 0; m < HN; ++m) {
-        const long long e = g0 + S::n1 * (h * HN + m);
-        q[m] = pin ? pin[e] : mk<float>(0.f, 0.f);
-        v[m] = pv[e];
-      }
-#pragma unroll
-      for (int m = 0; m < HN; ++m) {
-        const int n2 = h * HN + m;
-        const C o = newton_epi<float>(u[n2], v[m], q[m], alpha, beta);
-        pout[g0 + S::n1 * n2] = o;
-        u[n2] = o;
-      }
+    for (int n2 = 0; n2 < S::n2; ++n2) {
+      const C o = newton_epi<float>(u[n2], v[n2], q[n2], alpha, beta);
+      pout[g0 + S::n1 * n2] = o;
+      u[n2] = o;
     }
     if constexpr (FWD) {
       Dft<S::n2, -1, float>::run(u);
