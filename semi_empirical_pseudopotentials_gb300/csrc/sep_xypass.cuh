@@ -70,18 +70,19 @@ __device__ __forceinline__ int row_of_group(int j) {
 // inverse stage B' from global memory (g: the plane in position order, row
 // stride L): item (column, k2): positions k1 + N1 k2 -> inverse DFT_N1,
 // conjugate twiddle, back to the same positions in shared memory.  Adjacent
-// threads on adjacent columns; two items per thread loaded before either is
-// transformed.
+// threads on adjacent columns; a thread's items (four when they divide
+// evenly, else two at a time) are loaded before any is transformed.
 template <int L>
 __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __restrict__ g) {
   using S = XyShape<L>;
   constexpr int NI = L * S::n2;
-  for (int i0 = threadIdx.x; i0 < NI; i0 += 2 * S::nt) {
-    C v[2][S::n1];
+  constexpr int IB = NI % (4 * S::nt) == 0 ? 4 : 2;  // items loaded per batch
+  for (int i0 = threadIdx.x; i0 < NI; i0 += IB * S::nt) {
+    C v[IB][S::n1];
 #pragma unroll
-    for (int t = 0; t < 2; ++t) {
+    for (int t = 0; t < IB; ++t) {
       const int i = i0 + t * S::nt;
-      if (NI % (2 * S::nt) == 0 || i < NI) {
+      if (NI % (IB * S::nt) == 0 || i < NI) {
         const int col = i % L, k2 = i / L;
         const C* q = g + (long long)(S::n1 * k2) * L + col;
 #pragma unroll
@@ -89,9 +90,9 @@ __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __re
       }
     }
 #pragma unroll
-    for (int t = 0; t < 2; ++t) {
+    for (int t = 0; t < IB; ++t) {
       const int i = i0 + t * S::nt;
-      if (NI % (2 * S::nt) == 0 || i < NI) {
+      if (NI % (IB * S::nt) == 0 || i < NI) {
         const int col = i % L, k2 = i / L;
         Dft<S::n1, +1, float>::run(v[t]);
 #pragma unroll
