@@ -176,13 +176,14 @@ def subspace_gram(sep, ctx, psi_d, m, n, dv, peaks):
 
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum per pair, 128^3 complex64,
-# from the 12-pair capture summarised in profiles/line_pass_c64_128.md
+# from the captures summarised in profiles/line_pass_c64_128.md (12 pairs)
+# and profiles/xy_plane_pass_c64_128.md (6 pairs)
 TRAFFIC_PER_PAIR_128 = {"y_fwd": (201.354752e6 + 142.915584e6) / 12,
                         "z_fki": (201.357312e6 + 140.684032e6) / 12,
                         "y_inv": (201.346304e6 + 143.166208e6) / 12,
                         "x_inv_epi_fwd": (444.561152e6 + 351.911936e6) / 12,
-                        # profiles/xy_plane_pass_c64_128.md (12 pairs)
-                        "xy_inv_epi_fwd": (423.71968e6 + 348.552192e6) / 12}
+                        # profiles/xy_plane_pass_c64_128.md (6 pairs)
+                        "xy_inv_epi_fwd": (214.69952e6 + 147.428864e6) / 6}
 
 
 def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):
