@@ -82,3 +82,22 @@ def test_fused_xy_plane_pass_equals_the_line_passes(n):
     ctx.set_fusion(True)
     d = np.abs(fused - lines).max()
     assert np.array_equal(fused, lines), (d, d / np.abs(lines).max())
+
+
+@pytest.mark.parametrize("precision,ns", [("mixed", 21), ("f64", 20), ("mixed", 2)])
+def test_host_filter_in_chunks_equals_device_filter(precision, ns):
+    """sep_filter (host buffers) filters the pairs in a large chunk and a small
+    last one, with the copies on their own streams; sep_filter_dev filters all
+    pairs at once.  Same arithmetic per pair: the outputs are equal."""
+    torch = pytest.importorskip("torch")
+    ctx, pot, dv, n = _job((64, 64, 32), 7, precision)
+    vmin = float(pot.min())
+    nc, dE = 50, 40.0
+    ar, ai, zn = sep.coefficients([-1.0, -0.5], nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+    start = sep.start_states(-23, ns, n, dv)
+    host = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    sd = torch.from_numpy(start).cuda()
+    od = torch.empty((ns, 2, n), dtype=torch.float64, device="cuda")
+    ctx.filter_dev(sd.data_ptr(), ns, ar, zn, 4.0 / dE, vmin, od.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(host, od.cpu().numpy())
