@@ -79,7 +79,7 @@ def build(verbose=False, jobs=None):
         obj = os.path.join(BUILD, u + ".o")
         objs.append(obj)
         if _stale(obj, src, deps):
-            tasks.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off",
+            tasks.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread",
                           "-I" + os.path.join(cuda, "include"), "-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         list(ex.map(lambda c: _run(c, verbose), tasks))
@@ -90,8 +90,8 @@ def build(verbose=False, jobs=None):
         # --no-undefined: a symbol missing from the objects fails the build
         # here, not the first dlopen on a GPU machine
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs +
-             ["-L" + libdir, "-lcusolver", "-Xlinker", "-rpath," + libdir,
-              "-Xlinker", "--no-undefined"], verbose)
+             ["-L" + libdir, "-lcusolver", "-Xcompiler", "-pthread", "-Xlinker",
+              "-rpath," + libdir, "-Xlinker", "--no-undefined"], verbose)
     compat_src = os.path.join(CSRC, "sep_fdcompat.c")
     if os.path.exists(compat_src) and _stale(COMPAT_LIB, compat_src, deps + [LIB]):
         _run(["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-I" + os.path.join(ROOT, "include"),

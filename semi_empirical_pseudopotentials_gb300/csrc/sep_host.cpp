@@ -3,9 +3,15 @@
 // of operations so the results are identical on any IEEE-754 host.
 #include "sep_host.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
 
 namespace sep {
 namespace host {
@@ -18,7 +24,47 @@ constexpr double kTwoPi = 6.28318530717958647692;  // filter/fd.h TWOPI
 inline double gaussian(double x, double dt) { return std::sqrt(dt / kPi) * std::exp(-(x * x) * dt); }
 }  // namespace
 
-void leja_points(long nc, double* zre, double* zim) {
+namespace {
+
+// threads for the host numerics: the hardware threads, at most 16
+int host_threads() {
+  const unsigned h = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(16u, h));
+}
+
+// a reusable barrier for a fixed team of threads (spins with yields)
+class SpinBarrier {
+ public:
+  explicit SpinBarrier(int n) : n_(n) {}
+  void wait() {
+    const int g = gen_.load(std::memory_order_acquire);
+    if (count_.fetch_add(1, std::memory_order_acq_rel) == n_ - 1) {
+      count_.store(0, std::memory_order_relaxed);
+      gen_.fetch_add(1, std::memory_order_release);
+    } else {
+      while (gen_.load(std::memory_order_acquire) == g) std::this_thread::yield();
+    }
+  }
+
+ private:
+  int n_;
+  std::atomic<int> count_{0}, gen_{0};
+};
+
+// runs f(t) for t in [0, n) on n threads (the caller runs t = 0)
+template <typename F> void run_team(int n, F&& f) {
+  std::vector<std::thread> team;
+  for (int t = 1; t < n; ++t) team.emplace_back(f, t);
+  f(0);
+  for (auto& th : team) th.join();
+}
+
+// The Leja points of filter/coeff.c:83-134 (samp_points_ashkenazy).  The
+// candidates are split over a team of threads: each updates its share of the
+// log-distance sums and finds its first maximum, and the team takes the
+// maximum of those in thread order, which is the first maximum overall: the
+// same points as one sequential scan.
+void leja_compute(long nc, double* zre, double* zim) {
   // 32 nc candidates: 7/8 evenly spaced on [-2, 2], 1/8 at the origin (the
   // reference spreads them over an imaginary interval of zero width).
   const long total = 32 * nc;
@@ -31,30 +77,66 @@ void leja_points(long nc, double* zre, double* zim) {
   for (long k = 0; k < total - at_origin; ++k) re[k] = lo + (double)k * step;
   for (long k = total - at_origin; k < total; ++k)
     im[k] = im_lo + (double)(k - total + at_origin) * im_step;
-
-  auto update = [&](double pr, double pi, bool first) {
-    for (long k = 0; k < total; ++k) {
-      const double a = re[k] - pr, b = im[k] - pi;
-      const double d2 = a * a + b * b;
-      if (d2 < 1.0e-10) logsum[k] = -1.0e30;
-      else logsum[k] = first ? std::log(d2) : logsum[k] + std::log(d2);
-    }
-  };
   zre[0] = re[0];
   zim[0] = im[0];
-  update(zre[0], zim[0], true);
-  for (long j = 1; j < nc; ++j) {
-    long arg = 0;
-    double best = -2.0e30;
-    for (long k = 0; k < total; ++k)
-      if (logsum[k] > best) {
-        best = logsum[k];
-        arg = k;
+  const int T = (int)std::max<long>(1, std::min<long>(host_threads(), total / 4096));
+  std::vector<double> best_v(T);
+  std::vector<long> best_k(T);
+  SpinBarrier bar(T);
+  run_team(T, [&](int t) {
+    const long k0 = total * t / T, k1 = total * (t + 1) / T;
+    auto update = [&](double pr, double pi, bool first) {
+      for (long k = k0; k < k1; ++k) {
+        const double a = re[k] - pr, b = im[k] - pi;
+        const double d2 = a * a + b * b;
+        if (d2 < 1.0e-10) logsum[k] = -1.0e30;
+        else logsum[k] = first ? std::log(d2) : logsum[k] + std::log(d2);
       }
-    zre[j] = re[arg];
-    zim[j] = im[arg];
-    update(zre[j], zim[j], false);
+    };
+    update(re[0], im[0], true);
+    for (long j = 1; j < nc; ++j) {
+      long arg = k0;
+      double best = -2.0e30;
+      for (long k = k0; k < k1; ++k)
+        if (logsum[k] > best) {
+          best = logsum[k];
+          arg = k;
+        }
+      best_v[t] = best;
+      best_k[t] = arg;
+      bar.wait();
+      long g = best_k[0];
+      double gb = best_v[0];
+      for (int u = 1; u < T; ++u)
+        if (best_v[u] > gb) {
+          gb = best_v[u];
+          g = best_k[u];
+        }
+      if (gb <= -2.0e30) g = 0;  // no candidate above the floor: the scan's initial index
+      if (t == 0) {
+        zre[j] = re[g];
+        zim[j] = im[g];
+      }
+      bar.wait();  // the team has read best_v before the next round writes it
+      update(re[g], im[g], false);
+    }
+  });
+}
+}  // namespace
+
+void leja_points(long nc, double* zre, double* zim) {
+  // they depend on nc only: computed once per nc and process
+  static std::mutex mu;
+  static std::map<long, std::vector<double>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(nc);
+  if (it == cache.end()) {
+    std::vector<double> z(2 * (size_t)nc);
+    leja_compute(nc, z.data(), z.data() + nc);
+    it = cache.emplace(nc, std::move(z)).first;
   }
+  std::memcpy(zre, it->second.data(), sizeof(double) * nc);
+  std::memcpy(zim, it->second.data() + nc, sizeof(double) * nc);
 }
 
 void coefficients(long ms, long nc, double dE, double vmin, double dt, const double* el,
@@ -63,7 +145,10 @@ void coefficients(long ms, long nc, double dE, double vmin, double dt, const dou
   leja_points(nc, zn, zi.data());
   const double scale = (2.0 - (-2.0)) / dE;
   auto energy_of = [&](long j) { return (zn[j] + 2.0) / scale + vmin; };
-  for (long e = 0; e < ms; ++e) {
+  // the targets are independent: one thread per target (up to the team size)
+  const int T = (int)std::max<long>(1, std::min<long>(host_threads(), ms));
+  run_team(T, [&](int t) {
+  for (long e = t; e < ms; e += T) {
     double* cr = an_re + e * nc;
     double* ci = an_im + e * nc;
     cr[0] = gaussian(energy_of(0) - el[e], dt);
@@ -85,6 +170,7 @@ void coefficients(long ms, long nc, double dE, double vmin, double dt, const dou
       ci[j] = (-ci[0] - si) / w;
     }
   }
+  });
 }
 
 // L'Ecuyer's two multiplicative congruential streams, combined through a
