@@ -255,18 +255,19 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     CK(xy_prepare(c->g32));
     c->xy_ready = true;
   }
-  // chunks of pairs [first, first + count): at most Bc each; with host
-  // buffers the last chunk is small (8 pairs, or half of them), so that only
-  // its output copy is not under a filter (8 pairs filter at 0.94 of the rate
-  // of 32)
+  // chunks of pairs [first, first + count): at most Bc each.  With host
+  // buffers the last chunk is halved while it has 8 pairs or more (32 pairs:
+  // 16, 8, 4, 4), so that each chunk's output copy runs under the next
+  // chunk's filter even when the host copies are slow, and only the last
+  // few pairs' copy is not overlapped
   std::vector<std::pair<long long, long long>> chunks;
   for (long long b0 = 0; b0 < B; b0 += Bc) chunks.push_back({b0, std::min<long long>(Bc, B - b0)});
   if (host) {
-    const long long tail = std::min<long long>(8, B / 2);
-    auto& last = chunks.back();
-    if (tail > 0 && last.second > tail) {
-      last.second -= tail;
-      chunks.push_back({last.first + last.second, tail});
+    while (chunks.back().second >= 8) {
+      auto& last = chunks.back();
+      const long long second = last.second / 2;
+      last.second -= second;
+      chunks.push_back({last.first + last.second, second});
     }
   }
   const long long nchunks = (long long)chunks.size();
