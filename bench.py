@@ -260,8 +260,8 @@ def measured_peaks():
 
 def in13_case():
     """The reference's In13_P16 fixture (36^3, 65 atoms, 16 x 10 states, nc 1024)
-    end to end: GPU FP64 and mixed vs the oracle's CPU pipeline on the host
-    cores, against the published eval.dat."""
+    end to end: GPU FP64, mixed, and mixed with one FP64 refinement step vs the
+    oracle's CPU pipeline on the host cores, against the published eval.dat."""
     import semi_empirical_pseudopotentials_gb300 as sep
     from oracle import oracle as O
     from tests import fixture_in13
@@ -273,10 +273,12 @@ def in13_case():
     start = sep.start_states(f["seed"], int(f["ns"]), n, f["dv"])
     out = {"published_converged_in_window": int(win.sum())}
     pot = None
-    for prec in ("f64", "mixed"):
+    for tag, prec, refine in (("f64", "f64", 0), ("mixed", "mixed", 0),
+                              ("mixed_refine1", "mixed", 1)):
         ctx = sep.Context(f["dims"], f["steps"], precision=prec)
         pot = ctx.vbuild(f["xyz"], f["types"].astype(np.int32), f["tab_r"], f["tab_v_shifted"],
                          f["tab_n"], f["mins"], scale=f["strain_scale"], install=True)
+        ctx.set_refine(refine)
         ctx.pipeline(start, f["el"], int(f["nc"]), float(pot.min()))  # warm-up
         t0 = time.perf_counter()
         res = ctx.pipeline(start, f["el"], int(f["nc"]), float(pot.min()))
@@ -284,8 +286,8 @@ def in13_case():
         ev, sg = res["eval"], res["sigma"]
         err = [float(np.min(np.abs(ev - e))) for e in ref_ev[win]]
         mine = (ev > -0.25) & (ev < 0.0) & (sg < 1e-5)
-        out[prec] = {"seconds": dt_, "mkept": res["mkept"], "converged_in_window": int(mine.sum()),
-                     "max_abs_err_vs_published_Ha": max(err)}
+        out[tag] = {"seconds": dt_, "mkept": res["mkept"], "converged_in_window": int(mine.sum()),
+                    "max_abs_err_vs_published_Ha": max(err)}
         ctx.close()
     if O.lapack_available():
         cores = os.cpu_count() or 1

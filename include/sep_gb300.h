@@ -75,6 +75,16 @@ int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
  * passes per step instead of four; same arithmetic per line).  enable = 0
  * selects the four line passes.  Default 1. */
 int sep_ctx_set_fusion(sep_ctx *ctx, int enable);
+/* FP64 refinement steps (0..8, default 0) that sep_pipeline runs after
+ * Rayleigh-Ritz (filter/Hmat.c:11-86).  Each step extends the subspace with
+ * the residuals H psi - E psi of the Ritz pairs, made orthogonal to them and
+ * orthonormal (directions of negligible residuals dropped), and repeats the
+ * Rayleigh-Ritz diagonalisation in FP64: about squaring the eigenvalue error
+ * of each pair; the lowest mkept pairs of the extended space are kept.  No
+ * counterpart in the reference.  A step needs a second block of 2 mkept
+ * states on the device and is skipped when it does not fit.  The refinement
+ * time is counted in rayleigh_ritz_s. */
+int sep_ctx_set_refine(sep_ctx *ctx, int steps);
 
 /* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------
  * hpsi = T psi + V psi for nstates complex grids (interleaved complex128). */

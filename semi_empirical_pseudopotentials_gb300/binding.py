@@ -94,6 +94,7 @@ def lib():
         L.sep_form_factor_backward.argtypes = [dp, C.c_double, dp, dp]
         L.sep_ctx_set_subspace.argtypes = [vp, C.c_int]
         L.sep_ctx_set_fusion.argtypes = [vp, C.c_int]
+        L.sep_ctx_set_refine.argtypes = [vp, C.c_int]
         L.sep_subspace_gemm.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, C.c_double,
                                         C.c_int, dp]
         L.sep_subspace_rotate.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, dp]
@@ -354,6 +355,10 @@ class Context:
                                 _p(tab_v), tab_n.ctypes.data_as(lp), tab_r.shape[1], _p(mins),
                                 _p(out), 1 if install else 0))
         return out
+
+    def set_refine(self, steps):
+        """FP64 residual-subspace steps after Rayleigh-Ritz in pipeline() (0..8)."""
+        _check(lib().sep_ctx_set_refine(self.h, int(steps)))
 
     def set_fusion(self, enable):
         """Fused xy plane pass for complex64 Newton steps (nx = ny in 64/96/128)."""

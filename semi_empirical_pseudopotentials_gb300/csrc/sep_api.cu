@@ -140,6 +140,7 @@ sep_ctx::~sep_ctx() {
     if (g.exec) cudaGraphExecDestroy(g.exec);
   free_grid(g64);
   free_grid(g32);
+  w_refine.release();
   for (DevBuf* b : {&w_hist, &w_fft, &w_acc, &w_coef, &w_steps, &w_start, &w_out, &w_red,
                     &w_small, &w_states, &w_states2, &w_tmp, &w_solver, &w_gemm, &w_hpsi,
                     &w_ozA, &w_ozB, &w_ozP, &w_ozE})
@@ -516,6 +517,11 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
   double* hpsi = nullptr;  // H psi of the Ritz vectors, when it fits beside them
   RET(rayleigh_ritz_device(c, d_psi, k, eval, &hpsi));
   RET(normalize_device(c, d_psi, k, hpsi));  // main.c:122
+  for (int it = 0; it < c->refine_steps; ++it) {  // optional FP64 refinement
+    long k2 = k;
+    RET(refine_device(c, d_psi, k, m, eval, &hpsi, &k2));
+    k = k2;
+  }
   CK(cudaEventRecord(ev[4], c->stream));
   RET(sigma_device(c, d_psi, k, sige, hpsi));
   CK(cudaEventRecord(ev[5], c->stream));
@@ -607,6 +613,12 @@ int sep_time_passes(sep_ctx* c, long npairs, int reps, double* ms_out) {
   RET(check_ctx(c));
   if (!ms_out) return arg_fail("sep_time_passes: null argument");
   return time_passes_device(c, npairs, reps, ms_out);
+}
+
+int sep_ctx_set_refine(sep_ctx* c, int steps) {
+  if (!c || steps < 0 || steps > 8) return arg_fail("sep_ctx_set_refine: steps in [0, 8]");
+  c->refine_steps = steps;
+  return kOk;
 }
 
 int sep_ctx_set_fusion(sep_ctx* c, int enable) {

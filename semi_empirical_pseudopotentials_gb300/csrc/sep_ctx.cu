@@ -779,6 +779,55 @@ int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host,
   return kOk;
 }
 
+// One FP64 block step after Rayleigh-Ritz (no counterpart in the reference,
+// whose filter/main.c:118-142 stops at Hmat and sigma): the residuals
+// r_i = H psi_i - E_i psi_i of the k Ritz pairs are made orthogonal to psi
+// (twice) and orthonormal (ortho_device, which drops the directions of
+// residuals that are already negligible); Rayleigh-Ritz on [psi; r] in a
+// workspace of its own gives k + k2 pairs, and the k lowest replace psi.  For
+// a pair with residual norm sigma and gap delta the eigenvalue error goes
+// from about sigma^2 / delta to about its square.  Skipped when the device
+// cannot hold the extended block.
+int refine_device(sep_ctx* c, double* d_psi, long k, long m_cap, double* eval_host,
+                  double** hpsi, long* k_out) {
+  (void)m_cap;
+  const long long n = c->n;
+  *k_out = k;
+  const size_t row = sizeof(double) * (size_t)n;
+  const size_t room = (size_t)(0.5 * (double)free_device_bytes()) + c->w_refine.bytes;
+  const long kr = std::min<long>(k, (long)((long long)(room / row) - k));
+  if (kr < 1) return kOk;
+  RET(grow(c, c->w_refine, row * (size_t)(k + kr)));
+  double* Z = c->w_refine.as<double>();
+  double* R = Z + (size_t)k * n;
+  CK(cudaMemcpyAsync(Z, d_psi, row * (size_t)k, cudaMemcpyDeviceToDevice, c->stream));
+  RET(grow(c, c->w_small, sizeof(double) * (2 * (size_t)k * kr + (size_t)kr)));
+  double* P = c->w_small.as<double>();
+  double* Pt = P + (size_t)k * kr;
+  double* ed = Pt + (size_t)kr * k;
+  CK(cudaMemcpyAsync(ed, eval_host, sizeof(double) * kr, cudaMemcpyHostToDevice, c->stream));
+  if (hpsi && *hpsi) {
+    CK(residual_rows(Z, *hpsi, ed, kr, n, R, c->stream));
+  } else {
+    RET(apply_h_real(c, Z, R, kr));
+    CK(residual_rows(Z, R, ed, kr, n, R, c->stream));
+  }
+  RET(project_out(c, R, kr, Z, k, P, Pt));
+  RET(project_out(c, R, kr, Z, k, P, Pt));
+  long k2 = 0;
+  const int r = ortho_device(c, R, kr, &k2);
+  if (r == kErrNumeric) return kOk;  // all residuals vanish: nothing to add
+  if (r != kOk) return r;
+  RET(normalize_device(c, R, k2));
+  std::vector<double> ev((size_t)(k + k2));
+  RET(rayleigh_ritz_device(c, Z, k + k2, ev.data(), hpsi));
+  // the k lowest pairs (ascending) replace psi; H psi keeps its first k rows
+  CK(cudaMemcpyAsync(d_psi, Z, row * (size_t)k, cudaMemcpyDeviceToDevice, c->stream));
+  std::memcpy(eval_host, ev.data(), sizeof(double) * (size_t)k);
+  RET(normalize_device(c, d_psi, k, hpsi ? *hpsi : nullptr));
+  return kOk;
+}
+
 // filter/energy.c:88-119: sigma = sqrt(<H^2> - <H>^2) = |H psi - E psi| for a
 // normalised psi (dv metric) with E = <psi|H|psi>.
 int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,

@@ -73,6 +73,7 @@ struct sep_ctx {
   bool have_pot = false;
   bool use_graphs = true;
   int block_steps = 32;
+  int refine_steps = 0;  // FP64 residual-subspace steps after Rayleigh-Ritz in sep_pipeline
   int subspace_tc = 1;  // subspace contractions on the tensor cores (1) or the FP64 pipe (0)
   int fuse_xy = 1;      // complex64 Newton steps with the fused xy plane pass when it applies
   bool xy_ready = false;
@@ -81,6 +82,7 @@ struct sep_ctx {
   sep::GridDev<double> g64;
   sep::GridDev<float> g32;
   // workspace
+  sep::DevBuf w_refine;  // psi and its residual directions (refine_device)
   sep::DevBuf w_hist, w_fft, w_acc, w_coef, w_steps, w_start, w_out, w_red, w_small,
       w_states, w_states2, w_tmp, w_solver, w_gemm, w_hpsi, w_ozA, w_ozB, w_ozP, w_ozE;
   std::vector<sep::FilterGraph> graphs;
@@ -113,6 +115,12 @@ int release_filter_workspace_if_short(sep_ctx* c, size_t need);
 // *hpsi when the device has room for it, else *hpsi = nullptr
 int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host,
                          double** hpsi = nullptr);
+// One FP64 refinement step of k Ritz pairs (psi rows): the subspace grows by
+// the residuals H psi - E psi, made orthogonal to psi and orthonormal, and
+// the k lowest Ritz pairs of Rayleigh-Ritz on it replace psi (*k_out = k).
+// *hpsi: H psi of the rows when known (as rayleigh_ritz_device returns it).
+int refine_device(sep_ctx* c, double* d_psi, long k, long m_cap, double* eval_host,
+                  double** hpsi, long* k_out);
 // d_hpsi: H psi of these states when already known (no H applies then)
 int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,
                  const double* d_hpsi = nullptr);

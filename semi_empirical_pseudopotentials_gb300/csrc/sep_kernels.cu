@@ -729,6 +729,20 @@ cudaError_t residual_norms(const double* x, const double* hx, const double* e, l
   return cudaGetLastError();
 }
 
+__global__ void k_residual_rows(const double* __restrict__ x, const double* hx,
+                                const double* __restrict__ e, long long M, long long n,
+                                double* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M * n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = hx[i] - e[i / n] * x[i];
+}
+
+cudaError_t residual_rows(const double* x, const double* hx, const double* e, long long M,
+                          long long n, double* out, cudaStream_t s) {
+  k_residual_rows<<<blocks_for(M * n, kThreads), kThreads, 0, s>>>(x, hx, e, M, n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t convert_f32_to_f64(const float* in, double* out, long long count, cudaStream_t s) {
   k_convert<float, double><<<blocks_for(count, kThreads), kThreads, 0, s>>>(in, out, count);
   return cudaGetLastError();

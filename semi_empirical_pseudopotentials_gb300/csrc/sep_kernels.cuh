@@ -89,6 +89,9 @@ cudaError_t scale_eigvecs(const double* V, const double* lam, long long M, long 
 cudaError_t residual_norms(const double* x, const double* hx, const double* e, long long M,
                            long long n, double dv, double* out_dev, double* partial,
                            cudaStream_t s);
+// residual rows: out[m][g] = hx[m][g] - e[m] x[m][g] (out may alias hx)
+cudaError_t residual_rows(const double* x, const double* hx, const double* e, long long M,
+                          long long n, double* out, cudaStream_t s);
 // precision conversion
 cudaError_t convert_f32_to_f64(const float* in, double* out, long long count, cudaStream_t s);
 cudaError_t convert_f64_to_f32(const double* in, float* out, long long count, cudaStream_t s);
