@@ -77,7 +77,8 @@ int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
 int sep_ctx_set_fusion(sep_ctx *ctx, int enable);
 /* FP64 refinement steps (0..8, default 0) that sep_pipeline runs after
  * Rayleigh-Ritz (filter/Hmat.c:11-86).  Each step extends the subspace with
- * the residuals H psi - E psi of the Ritz pairs, made orthogonal to them and
+ * the residuals H psi - E psi of the Ritz pairs (preconditioned with
+ * (T + 1 Ha)^-1 in complex64 contexts), made orthogonal to them and
  * orthonormal (directions of negligible residuals dropped), and repeats the
  * Rayleigh-Ritz diagonalisation in FP64: about squaring the eigenvalue error
  * of each pair; the lowest mkept pairs of the extended space are kept.  No

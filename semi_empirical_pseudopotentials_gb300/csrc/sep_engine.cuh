@@ -53,6 +53,7 @@ template <typename T> struct PassIO {
   const T* coefs = nullptr;  // device (alpha, beta) per step
   int step = 0;
   int variant = -1;          // -1: the grid's autotuned choice
+  T pc_a = T(0), pc_b = T(0);  // z pass: 1 / (pc_a k + pc_b) instead of k when pc_a != 0
 };
 
 // One line pass over a batch of B grids (see sep_fftpass.cuh for modes).
@@ -76,6 +77,12 @@ cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& 
 template <typename T>
 cudaError_t apply_txvy(const GridDev<T>& g, const cx<T>* x, const cx<T>* y, cx<T>* out,
                        cx<T>* scratch, int B, T alpha, T beta, cudaStream_t s);
+
+// Kinetic preconditioner on B complex grids: out = (T + shift)^-1 in, T the
+// capped kinetic operator of the grid.  scratch: B * n complex.
+template <typename T>
+cudaError_t apply_precond(const GridDev<T>& g, const cx<T>* in, cx<T>* out, cx<T>* scratch,
+                          int B, double shift, cudaStream_t s);
 
 // H (or alpha H + beta) applied to B complex grids: out = alpha (T in + V in) + beta in.
 // scratch: B * n complex.  out may not alias in.

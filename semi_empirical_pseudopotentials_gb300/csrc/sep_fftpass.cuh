@@ -30,6 +30,7 @@ enum PassMode : int {
   kFwdKInv = 2,     // forward, multiply by the k^2 table, backward (z axis)
   kInvEpi = 3,      // backward, then out = alpha (u + V psi_in) + beta psi_in (x axis)
   kInvEpiFwd = 4,   // kInvEpi, then forward transform of out back into data (x axis)
+  kFwdPInv = 5,     // forward, multiply by 1 / (pc_a k^2 + pc_b), backward (z axis)
 };
 
 template <typename T> struct PassArgs {
@@ -43,6 +44,7 @@ template <typename T> struct PassArgs {
   const T* ky;
   const T* kz;
   T kcap;                 // Ekinmax / N (filter/init.c:137-143)
+  T pc_a, pc_b;           // kFwdPInv: multiply by 1 / (pc_a k + pc_b) (kinetic preconditioner)
   T alpha, beta;          // epilogue scalars, unless coefs is set
   const T* coefs;         // epilogue: device (alpha, beta) pairs, entry `step`
   int step;
@@ -287,8 +289,9 @@ line_pass(PassArgs<T> a) {
     __syncthreads();
     inverse_from_vb();
     storeA(a.data);
-  } else if constexpr (MODE == kFwdKInv) {
+  } else if constexpr (MODE == kFwdKInv || MODE == kFwdPInv) {
     static_assert(AXIS == 2, "k^2 multiply is fused into the z pass");
+    constexpr bool PRECOND = MODE == kFwdPInv;
     loadA(a.data);
     __syncthreads();
     forward_from_va();
@@ -304,6 +307,7 @@ line_pass(PassArgs<T> a) {
       for (int k1 = 0; k1 < N1; ++k1) {
         T k = kxy + a.kz[k2 + N2 * k1];
         k = (k > a.kcap) ? a.kcap : k;
+        if constexpr (PRECOND) k = T(1) / (a.pc_a * k + a.pc_b);
         vb[r][k1] = scale<T>(vb[r][k1], k);
       }
     }

@@ -35,6 +35,8 @@ cudaError_t launch_len(int axis, int mode, const PassArgs<T>& a, int B, cudaStre
     if (mode == kInv) return launch_one<T, L, 1, kInv, V>(a, B, s);
   } else if (axis == 2) {
     if (mode == kFwdKInv) return launch_one<T, L, 2, kFwdKInv, V>(a, B, s);
+    if constexpr (sizeof(T) == 8)  // the preconditioner of the FP64 refinement
+      if (mode == kFwdPInv) return launch_one<T, L, 2, kFwdPInv, V>(a, B, s);
   }
   return cudaErrorInvalidValue;
 }
@@ -80,6 +82,8 @@ cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
   a.kcap = g.kcap;
   a.alpha = io.alpha;
   a.beta = io.beta;
+  a.pc_a = io.pc_a;
+  a.pc_b = io.pc_b;
   a.nbatch_lines = (long long)B * g.ny * g.nz;
   a.nx = g.nx;
   a.ny = g.ny;
@@ -127,6 +131,31 @@ cudaError_t apply_h<SEP_T>(const GridDev<SEP_T>& g, const cx<SEP_T>* in, cx<SEP_
   io.psi_out = out;
   io.alpha = alpha;
   io.beta = beta;
+  return run_pass<SEP_T>(0, kInvEpi, g, io, B, s);
+}
+
+template <>
+cudaError_t apply_precond<SEP_T>(const GridDev<SEP_T>& g, const cx<SEP_T>* in, cx<SEP_T>* out,
+                                 cx<SEP_T>* scratch, int B, double shift, cudaStream_t s) {
+  // the k tables carry 1/N and the transform pair a factor N: multiplying by
+  // 1 / (N^2 k + N shift) leaves (T + shift)^-1
+  cudaError_t e;
+  const double nn = (double)g.n;
+  PassIO<SEP_T> io;
+  io.data = scratch;
+  io.src = in;
+  if ((e = run_pass<SEP_T>(0, kFwd, g, io, B, s))) return e;
+  io.src = nullptr;
+  if ((e = run_pass<SEP_T>(1, kFwd, g, io, B, s))) return e;
+  io.pc_a = (SEP_T)(nn * nn);
+  io.pc_b = (SEP_T)(nn * shift);
+  if ((e = run_pass<SEP_T>(2, kFwdPInv, g, io, B, s))) return e;
+  io.pc_a = io.pc_b = (SEP_T)0;
+  if ((e = run_pass<SEP_T>(1, kInv, g, io, B, s))) return e;
+  io.psi_in = nullptr;  // epilogue with no V term: out = the transformed grid
+  io.psi_out = out;
+  io.alpha = (SEP_T)1;
+  io.beta = (SEP_T)0;
   return run_pass<SEP_T>(0, kInvEpi, g, io, B, s);
 }
 

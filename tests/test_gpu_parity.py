@@ -250,11 +250,10 @@ def test_in13_fixture_end_to_end():
 def test_in13_mixed_precision_with_fp64_refinement(refine):
     """The complex64 filter path on In13_P16.  Without refinement its Ritz
     values are within a few 1e-6 Ha of the published eval.dat (measured:
-    2.9e-6); one FP64 residual-subspace step after Rayleigh-Ritz brings every
-    published converged state in [-0.25, 0] Ha within 1e-6 Ha (measured:
-    7e-7).  The residual norms of the mixed path stay above 1e-5: the filter's
-    single-precision noise is spread over the whole spectrum, and an
-    unpreconditioned step removes it slowly."""
+    2.9e-6); one FP64 step after Rayleigh-Ritz (kinetically preconditioned
+    residuals) brings every published converged state in [-0.25, 0] Ha within
+    1e-6 Ha (measured: 1.1e-7).  Its residual norms fall more slowly (median
+    1.2e-4, then 4e-5 after one step and 5e-6 after three)."""
     from tests import fixture_in13
 
     f = fixture_in13.load()
