@@ -29,7 +29,8 @@ enum sep_status {
   SEP_ERR_NOMEM = -3,        /* device allocation failed */
   SEP_ERR_SOLVER = -4,       /* dense eigensolver failed (reference: dsyev/dgesvd info) */
   SEP_ERR_NO_DEVICE = -5,    /* no CUDA device / library built without one */
-  SEP_ERR_NUMERIC = -6       /* non-finite values, empty subspace */
+  SEP_ERR_NUMERIC = -6,      /* non-finite values, empty subspace */
+  SEP_ERR_IO = -7            /* a file could not be read or written */
 };
 
 enum sep_precision {
@@ -298,6 +299,46 @@ int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
  *    ordered by the caller) share the scratch and race: serialise them. */
 int sep_normalize_states_noalloc(double *psi_dev, long m, long ngrid, double dv,
                                  void *cuda_stream);
+
+/* ---- output files ---------------------------------------------------------
+ * Byte for byte what the reference's stdio calls write; no device needed.
+ * sep_write_states: m raw FP64 state blocks of ngrid values, no header
+ *   (psi.dat, filter/main.c:129-131; psi-filt-<tid>-<jns>.dat,
+ *   filter/filter.c:44-47).  Large files are written by a team of threads.
+ * sep_write_eval: "%ld %.16g %g\n" = index, E, sigma per line (eval.dat,
+ *   filter/main.c:138-142).
+ * sep_write_filter_eval: "%ld %.16g %.16g\n" = index, E, target per line
+ *   (eval-filt-<tid>-<jns>.dat, filter/filter.c:37-41).
+ * SEP_ERR_IO when a file cannot be created or written. */
+int sep_write_states(const char *path, const double *psi, long m, long ngrid);
+int sep_write_eval(const char *path, const double *eval, const double *sige, long m);
+int sep_write_filter_eval(const char *path, const double *eval, const double *el, long ms);
+
+/* ---- merge of several filter runs (combine_filter_outputs.py) -------------
+ * The step between the filter and bse/: reads eval_name (default eval.dat)
+ * and psi_name (default psi.dat) in each of the ndatasets directories, sorts
+ * every state by (E, sigma, run, index in run) and writes into output_dir
+ * (default merged_filter, created with its parents):
+ *   eval.par             "%d %.16g %.16g\n" with the new indices;
+ *   psi.par              the state blocks in the new order;
+ *   merge_manifest.txt   ngrid, nstates, the sources and the mapping;
+ *   conf.par             a copy of the first run's, when copy_conf != 0.
+ * The checks and messages are the script's (combine_filter_outputs.py:
+ * 125-214, 250-263): a missing file, a line with fewer than 3 columns or a
+ * field that Python's int()/float() rejects, an empty eval file, an
+ * input.par whose nx ny nz disagree with ngrid, a psi file whose size is not
+ * nstates x ngrid doubles, indices not 0..n-1, conf.par files that differ,
+ * copy_conf without a first conf.par.  Those return SEP_ERR_ARG with the
+ * script's message in sep_last_error(); a file that cannot be opened, read
+ * or written returns SEP_ERR_IO.  nstates (ndatasets entries) and total may
+ * be NULL.  The state blocks are copied by a team of threads. */
+int sep_combine_outputs(int ndatasets, const char *const *dirs, const char *eval_name,
+                        const char *psi_name, long ngrid, const char *output_dir,
+                        int copy_conf, long *nstates, long *total);
+/* nx*ny*nz from the first three integers of an input.par (filter or bse),
+ * combine_filter_outputs.py:125-145; SEP_ERR_ARG with the script's message
+ * when they are missing, not integers or not positive. */
+int sep_read_grid_source(const char *path, long *ngrid);
 
 #ifdef __cplusplus
 }

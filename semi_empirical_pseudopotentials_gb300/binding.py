@@ -104,6 +104,13 @@ def lib():
                                                 dp, dp]
         L.sep_band_edge_backward.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, C.c_double,
                                              dp, dp, C.c_long, dp, dp]
+        cp = C.c_char_p
+        L.sep_write_states.argtypes = [cp, dp, C.c_long, C.c_long]
+        L.sep_write_eval.argtypes = [cp, dp, dp, C.c_long]
+        L.sep_write_filter_eval.argtypes = [cp, dp, dp, C.c_long]
+        L.sep_read_grid_source.argtypes = [cp, lp]
+        L.sep_combine_outputs.argtypes = [C.c_int, C.POINTER(cp), cp, cp, C.c_long, cp, C.c_int,
+                                          lp, lp]
         _lib = L
     return _lib
 

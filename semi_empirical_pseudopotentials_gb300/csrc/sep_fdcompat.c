@@ -172,17 +172,9 @@ void filtering(double *psitot, double *potl, double *ksqr, zomplex *an, double *
   OK("energy_all", sep_energy_all(c, psitot, ms, eval));
   char str[100];
   snprintf(str, sizeof str, "eval-filt-%ld-%ld.dat", tid, jns);
-  FILE *pf = fopen(str, "w");
-  if (pf) {
-    for (long e = 0; e < ms; e++) fprintf(pf, "%ld %.16g %.16g\n", e, eval[e], el[e]);
-    fclose(pf);
-  }
+  OK("filtering", sep_write_filter_eval(str, eval, el, ms));
   snprintf(str, sizeof str, "psi-filt-%ld-%ld.dat", tid, jns);
-  pf = fopen(str, "w");
-  if (pf) {
-    fwrite(psitot, sizeof(double), (size_t)ms * n, pf);
-    fclose(pf);
-  }
+  OK("filtering", sep_write_states(str, psitot, ms, n));
   free(psi);
   free(eval);
 }

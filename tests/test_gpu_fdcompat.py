@@ -77,8 +77,13 @@ def test_reference_main_flow(golden, tmp_path, monkeypatch):
         L.filtering(blk, potl.ctypes.data_as(dp), ksqr.ctypes.data_as(dp),
                     an.ctypes.data_as(dp), zn.ctypes.data_as(dp), el.ctypes.data_as(dp), ist,
                     par, C.c_long(0), C.c_long(s), C.byref(idum))
-    assert os.path.exists(tmp_path / "eval-filt-0-3.dat")
-    assert os.path.getsize(tmp_path / "psi-filt-0-3.dat") == ms * N * 8
+    # the per-cycle files of filter/filter.c:37-47: the filtered block as raw
+    # doubles, and "%ld %.16g %.16g" lines of (index, E, target)
+    assert np.array_equal(np.fromfile(tmp_path / "psi-filt-0-3.dat"),
+                          psitot[3 * ms * N:4 * ms * N])
+    rows = np.loadtxt(tmp_path / "eval-filt-0-3.dat", ndmin=2)
+    assert np.array_equal(rows[:, 0], np.arange(ms))
+    assert np.allclose(rows[:, 2], el, rtol=1e-15, atol=0)
     ist.mstot = L.portho(psitot.ctypes.data_as(dp), C.c_double(par.dv), ist)   # main.c:110
     assert ist.mstot == len(g["run_eval"])
     L.normalize_all(psitot.ctypes.data_as(dp), C.c_double(par.dv), C.c_long(ist.mstot),
