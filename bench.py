@@ -304,6 +304,53 @@ def in13_case():
     return out
 
 
+def bulk_case(reps=5):
+    """The reference's two-crystal bulk fit (pseudopotFitting/TESTS/cdse:
+    wurtzite CdSe, 42 k-points x 377 plane waves, and zincblende CdSe, 20 x
+    387): the fit objective (both band structures) and its gradient on the GPU,
+    with the batched and the per-matrix eigensolver, against the oracle's band
+    structures (numpy eigvalsh) on the host cores."""
+    import tempfile
+
+    from oracle import bulk_oracle as bo
+    from semi_empirical_pseudopotentials_gb300 import bulk
+    from tests import fixture_bulk as fb
+
+    with tempfile.TemporaryDirectory() as d:
+        fit = bulk.read_fit_inputs(fb.materialise("cdse", d))
+    best = fb.best_atom_params("cdse")
+    theta = np.array([best[0][0], best[0][2]])
+    bf = bulk.BulkFit(fit)
+    out = {"crystals": [{"nk": bc.nk, "plane_waves": bc.nbv, "bands": bc.nev}
+                        for bc in bf.crystals]}
+
+    def timed(f):
+        f()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            f()
+        return (time.perf_counter() - t0) / reps
+
+    out["objective_s"] = timed(lambda: bf.objective(theta))
+    out["objective_and_gradient_s"] = timed(lambda: bf.objective_and_grad(theta))
+    out["solver"] = ["batched" if bc.solver_path == 1 else "per-matrix" for bc in bf.crystals]
+    for bc in bf.crystals:
+        bc.set_solver(False)
+    out["objective_per_matrix_solver_s"] = timed(lambda: bf.objective(theta))
+    bands = bf.band_structures(theta)
+    out["max_abs_err_vs_published_eV"] = max(
+        float(np.abs(b - fb.published_bands("cdse", i)[1]).max()) for i, b in enumerate(bands))
+    t0 = time.perf_counter()
+    for ci, c in enumerate(fit.crystals):
+        bo.bands(c.cell, c.tau, best[ci], c.kpts, c.max_ke, c.ne, fit.ke_scale)
+    t_cpu = time.perf_counter() - t0
+    out["cpu_port"] = {"objective_s": t_cpu, "cores": os.cpu_count() or 1,
+                       "kind": "port (numpy eigvalsh per k-point, in place of zheev)"}
+    out["speedup_gpu_over_cpu"] = t_cpu / out["objective_s"]
+    bf.close()
+    return out
+
+
 def cpu_baseline(S, pot, dE, an_re, zn, vmin, seconds=12.0):
     """The oracle's filter cycles on the host cores (bounded sample)."""
     from oracle import oracle as O
@@ -544,6 +591,7 @@ def run_sep(args):
         extras["time_to_band_edge"] = ttb
         ctx64.close()
         extras["in13_p16_fixture"] = in13_case()
+        extras["bulk_fit_cdse"] = bulk_case()
         extras["cpu_baseline"] = cpu_baseline(S, pot, dE, an_re, zn, vmin)
 
     if rank == 0:

@@ -340,6 +340,42 @@ int sep_combine_outputs(int ndatasets, const char *const *dirs, const char *eval
  * when they are missing, not integers or not positive. */
 int sep_read_grid_source(const char *path, long *ngrid);
 
+/* ---- bulk band structures and their gradient (pseudopotFitting/) ---------
+ * The empirical-pseudopotential fit to bulk band structures.  No device work
+ * in sep_bulk_basis.
+ * sep_bulk_basis: the plane waves G = i b0 + j b1 + k b2 with |G|^2 / 2 <
+ *   max_ke for the cell rows a0, a1, a2 (bohr; init.c:21-45,
+ *   states.c:10-61), ordered by |G|.  g == NULL: *nbv only; else g holds
+ *   cap >= *nbv vectors (x, y, z).
+ * sep_bulk_create: one crystal on the calling thread's device: nbv plane
+ *   waves g, natom atoms tau (bohr) with types[a] in [0, ntype), ntype <= 8,
+ *   nk k-points (bohr^-1), the kinetic scale s of H = s |k+G|^2 / 2 + V
+ *   (input.par kineticEnergyScaling) and nev <= nbv bands kept per k-point.
+ * sep_bulk_bands: params = ntype x {a0, a1, a2, a3} of
+ *   v(q) = a0 (q^2 - a1) / (a2 exp(a3 q^2) + 1) (hamiltonian.c:91-94);
+ *   bands = nk x nev lowest eigenvalues in eV (fit.c:71-97: V once, H_k for
+ *   all k-points, one batched Hermitian eigensolve).
+ * sep_bulk_bands_backward: given dL/dE (nk x nev, per eV), writes
+ *   dL/dparams (ntype x 4) by Hellmann-Feynman (no reference counterpart:
+ *   the reference fits by Monte Carlo, fit.c:9-69), and the bands when
+ *   bands != NULL.  Degenerate bands must carry equal dL/dE for the result
+ *   to be the gradient.
+ * sep_bulk_solver_path: 1 when the batched eigensolver ran, 0 when the
+ *   matrices went one per call, -1 before the first solve.
+ * sep_bulk_set_solver: 1 (default) = the batched eigensolver, one matrix per
+ *   call where it declines the size; 0 = one matrix per call. */
+typedef struct sep_bulk sep_bulk;
+int sep_bulk_basis(const double cell[9], double max_ke, long cap, long *nbv, double *g);
+int sep_bulk_create(long nbv, const double *g, long natom, const double *tau, const int *types,
+                    long ntype, long nk, const double *kpts, double ke_scale, long nev,
+                    sep_bulk **out);
+int sep_bulk_bands(sep_bulk *b, const double *params, double *bands);
+int sep_bulk_bands_backward(sep_bulk *b, const double *params, const double *dl_de,
+                            double *bands, double *dl_dparams);
+int sep_bulk_solver_path(sep_bulk *b, int *batched);
+int sep_bulk_set_solver(sep_bulk *b, int batched);
+int sep_bulk_destroy(sep_bulk *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,6 +111,14 @@ def lib():
         L.sep_read_grid_source.argtypes = [cp, lp]
         L.sep_combine_outputs.argtypes = [C.c_int, C.POINTER(cp), cp, cp, C.c_long, cp, C.c_int,
                                           lp, lp]
+        L.sep_bulk_basis.argtypes = [dp, C.c_double, C.c_long, lp, dp]
+        L.sep_bulk_create.argtypes = [C.c_long, dp, C.c_long, dp, ip, C.c_long, C.c_long, dp,
+                                      C.c_double, C.c_long, C.POINTER(vp)]
+        L.sep_bulk_bands.argtypes = [vp, dp, dp]
+        L.sep_bulk_bands_backward.argtypes = [vp, dp, dp, dp, dp]
+        L.sep_bulk_solver_path.argtypes = [vp, ip]
+        L.sep_bulk_set_solver.argtypes = [vp, C.c_int]
+        L.sep_bulk_destroy.argtypes = [vp]
         _lib = L
     return _lib
 

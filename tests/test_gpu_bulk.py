@@ -1,0 +1,139 @@
+"""Bulk band structures and their gradient on the GPU (sep_bulk_*, through
+the C ABI) against the oracle (oracle/bulk_oracle.py) and the reference's
+published runs (tests/golden/bulk_fit.json)."""
+import numpy as np
+import pytest
+
+from oracle import bulk_oracle as bo
+from semi_empirical_pseudopotentials_gb300 import bulk
+from tests import fixture_bulk as fb
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def fits(tmp_path_factory):
+    return {run: bulk.read_fit_inputs(fb.materialise(run, str(tmp_path_factory.mktemp(run))))
+            for run in ("zb_cdse", "w_cdse", "cdse")}
+
+
+@pytest.mark.parametrize("run,i", [("zb_cdse", 0), ("w_cdse", 0), ("cdse", 1)])
+def test_bands_match_oracle_and_published(fits, run, i):
+    c = fits[run].crystals[i]
+    bc = bulk.BulkCrystal(c, fits[run].ke_scale)
+    p = bc.type_params(fb.best_atom_params(run)[i])
+    got = bc.bands(p)
+    ref = bo.bands(c.cell, c.tau, fb.best_atom_params(run)[i], c.kpts, c.max_ke, c.ne,
+                   fits[run].ke_scale)
+    assert np.abs(got - ref).max() < 1e-8                # eV
+    assert np.abs(got - fb.published_bands(run, i)[1]).max() < 1.2e-5
+    bc.close()
+
+
+def test_solver_paths_agree(fits):
+    c = fits["w_cdse"].crystals[0]
+    bc = bulk.BulkCrystal(c)
+    p = bc.type_params(fb.best_atom_params("w_cdse")[0])
+    a = bc.bands(p)
+    path = bc.solver_path
+    bc.set_solver(False)
+    b = bc.bands(p)
+    assert bc.solver_path == 0 and path in (0, 1)
+    assert np.abs(a - b).max() < 1e-9
+    bc.close()
+
+
+def cluster_weights(e_full, nev, rng):
+    """Per k-point weights that are equal inside each cluster of degenerate
+    bands (so that the weighted sum of bands is differentiable); a cluster
+    that reaches past band nev gets weight 0."""
+    w = np.zeros((e_full.shape[0], nev))
+    for k in range(e_full.shape[0]):
+        n = 0
+        while n < nev:
+            m = n + 1
+            while m < e_full.shape[1] and e_full[k, m] - e_full[k, m - 1] < 1e-3:
+                m += 1
+            if m <= nev:
+                w[k, n:m] = rng.uniform(0.5, 1.5)
+            n = m
+    return w
+
+
+# the oracle's differences for every parameter of zb_cdse, for a0 of each
+# element of w_cdse (one oracle evaluation there takes about a second)
+@pytest.mark.parametrize("run,oracle_params", [("zb_cdse", (0, 1, 2, 3)), ("w_cdse", (0,))])
+def test_gradient_matches_reference_derived_differences(fits, run, oracle_params):
+    c = fits[run].crystals[0]
+    bc = bulk.BulkCrystal(c)
+    atom_p = fb.best_atom_params(run)[0]
+    p = bc.type_params(atom_p)
+    full = bo.bands(c.cell, c.tau, atom_p, c.kpts, c.max_ke, c.ne + 2)
+    w = cluster_weights(full, c.ne, np.random.default_rng(7))
+    _, grad = bc.backward(p, w)
+    types = [bc.types_of.index(s) for s in c.symbols]
+
+    def loss_oracle(pp):
+        return float(np.sum(w * bo.bands(c.cell, c.tau, pp[types], c.kpts, c.max_ke, c.ne)))
+
+    def loss_gpu(pp):
+        return float(np.sum(w * bc.bands(pp)))
+
+    # with h = 1e-6 the bands move by about 1e-4 eV, far less than the 1 meV
+    # that separates the weight clusters
+    h = 1e-6
+    fd_ref, fd_gpu = np.full_like(p, np.nan), np.zeros_like(p)
+    for t in range(p.shape[0]):
+        for m in range(4):
+            e = np.zeros_like(p)
+            e[t, m] = h
+            fd_gpu[t, m] = (loss_gpu(p + e) - loss_gpu(p - e)) / (2 * h)
+            if m in oracle_params:
+                fd_ref[t, m] = (loss_oracle(p + e) - loss_oracle(p - e)) / (2 * h)
+    scale = np.abs(fd_gpu).max()
+    sel = ~np.isnan(fd_ref)
+    assert np.abs(grad - fd_ref)[sel].max() < 1e-6 * scale, (grad, fd_ref)
+    assert np.abs(grad - fd_gpu).max() < 1e-6 * scale, (grad, fd_gpu)
+    bc.close()
+
+
+def test_fit_objective_and_gradient(fits):
+    fit = fits["cdse"]
+    bf = bulk.BulkFit(fit)
+    best = fb.best_atom_params("cdse")
+    theta = np.array([best[0][0], best[0][2]])
+    val, grad = bf.objective_and_grad(theta)
+    # the oracle's objective (fit.c:101-122) on the same crystal parameters
+    ref = np.mean([bo.weighted_mse(
+        bo.bands(c.cell, c.tau, [bulk.fit_atom_params(fit, theta, ci, s) for s in c.symbols],
+                 c.kpts, c.max_ke, c.ne), c.exp_bands) for ci, c in enumerate(fit.crystals)])
+    assert abs(val - ref) < 1e-9 * ref
+    assert abs(bf.objective(theta) - val) < 1e-12 * val
+    # the chain to the shared parameters: sum of each crystal's gradient
+    manual = np.zeros_like(theta)
+    for ci, (bc, p) in enumerate(zip(bf.crystals, bf.crystal_params(theta))):
+        b = bc.bands(p)
+        _, d = bf._mse_terms(ci, b)
+        _, gp = bc.backward(p, d / len(bf.crystals))
+        for t, s in enumerate(bc.types_of):
+            f = gp[t].copy()
+            if ci == 1:
+                f[0] *= fit.norm_vol[1] / fit.norm_vol[0]
+            manual[fit.elements.index(s)] += f
+    assert np.allclose(grad, manual, rtol=1e-12, atol=0)
+    torch = pytest.importorskip("torch")
+    th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
+    loss = bulk.BandStructureMSE.apply(th, bf)
+    loss.backward()
+    assert abs(loss.item() - val) < 1e-12 * val
+    assert np.allclose(th.grad.numpy(), grad, rtol=1e-12, atol=0)
+    bf.close()
+
+
+def test_bad_arguments_are_reported():
+    with pytest.raises(bulk.SepError):
+        bulk.basis(np.zeros(9), 5.0)
+    c = bulk.Crystal(cell=np.eye(3) * 10.0, symbols=["X"], tau=np.zeros((1, 3)),
+                     kpts=np.zeros((1, 3)), max_ke=1.0, ne=10 ** 6, scale=10.0)
+    with pytest.raises(bulk.SepError):
+        bulk.BulkCrystal(c)
