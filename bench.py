@@ -351,6 +351,66 @@ def bulk_case(reps=5):
     return out
 
 
+def spinor_case(reps=5):
+    """The spin-orbit operator of the spinor filter (Gaussian and
+    Kleinman-Bylander forms, spinors/filterSpinors/hamiltonian.c:81-401) on
+    a 96^3 grid (0.5 bohr) with 300 atoms, about 590 neighbour points each:
+    device time per apply (CUDA events) against the oracle on the host."""
+    import ctypes as C
+
+    import torch
+
+    from oracle import spinor_oracle as so
+    from semi_empirical_pseudopotentials_gb300 import binding
+
+    rng = np.random.default_rng(17)
+    n, h, natom = 96, 0.5, 300
+    v = -0.5 * n * h + h * np.arange(n)
+    rxyz = rng.uniform(-20.0, 20.0, size=(natom, 3))
+    nlc, nl = so.neighbour_lists(v, v, v, rxyz, rng.uniform(-0.1, 0.1, natom),
+                                 0.49 * 6.0 * np.log(10.0), 700)
+    nlc["Vs0G1"] = rng.normal(size=nlc.shape)
+    nlc["Vs0G_2"] = rng.normal(size=nlc.shape)
+    ng = n ** 3
+    psi = rng.normal(size=2 * ng) + 1j * rng.normal(size=2 * ng)
+    elkb = rng.uniform(0.5, 2.0, 2 * natom)
+    dev = torch.device("cuda:0")
+    d_psi = torch.from_numpy(psi.view(np.float64).copy()).to(dev)
+    d_nlc = torch.from_numpy(np.ascontiguousarray(nlc).view(np.uint8).reshape(-1).copy()).to(dev)
+    d_nl = torch.from_numpy(nl.astype(np.int64)).to(dev)
+    d_el = torch.from_numpy(elkb).to(dev)
+    d_out = torch.empty_like(d_psi)
+    L = binding.lib()
+    out = {"grid": f"{n}^3", "atoms": natom, "points_per_atom": float(nl.mean())}
+    stream = torch.cuda.current_stream()
+    for form, kb in (("gauss", 0), ("kb", 1)):
+        def call():
+            st = L.sep_spinor_vso_dev(C.c_void_p(d_psi.data_ptr()), ng, natom, nlc.shape[1],
+                                      C.c_void_p(d_nlc.data_ptr()), C.c_void_p(d_nl.data_ptr()),
+                                      h, h ** 3, kb, C.c_void_p(d_el.data_ptr()),
+                                      C.c_void_p(d_out.data_ptr()),
+                                      C.c_void_p(stream.cuda_stream))
+            if st != 0:
+                raise RuntimeError(L.sep_last_error().decode())
+        call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gpu_ms = e0.elapsed_time(e1) / reps
+        got = d_out.cpu().numpy().view(np.complex128)
+        t0 = time.perf_counter()
+        ref = (so.vso_gauss(psi, nlc, nl, h, h ** 3, ng) if not kb
+               else so.vso_kb(psi, nlc, nl, elkb, h ** 3, ng))
+        cpu_s = time.perf_counter() - t0
+        out[form] = {"gpu_ms": gpu_ms, "cpu_port_s": cpu_s, "speedup": cpu_s * 1e3 / gpu_ms,
+                     "max_rel_err_vs_oracle": float(np.abs(got - ref).max() / np.abs(ref).max())}
+    return out
+
+
 def cpu_baseline(S, pot, dE, an_re, zn, vmin, seconds=12.0):
     """The oracle's filter cycles on the host cores (bounded sample)."""
     from oracle import oracle as O
@@ -592,6 +652,10 @@ def run_sep(args):
         ctx64.close()
         extras["in13_p16_fixture"] = in13_case()
         extras["bulk_fit_cdse"] = bulk_case()
+        try:
+            extras["spinor_vso"] = spinor_case()
+        except Exception as exc:  # the operator's numbers are an extra, not the bench line
+            extras["spinor_vso"] = {"error": f"{type(exc).__name__}: {exc}"}
         extras["cpu_baseline"] = cpu_baseline(S, pot, dE, an_re, zn, vmin)
 
     if rank == 0:

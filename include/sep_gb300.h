@@ -376,6 +376,35 @@ int sep_bulk_solver_path(sep_bulk *b, int *batched);
 int sep_bulk_set_solver(sep_bulk *b, int batched);
 int sep_bulk_destroy(sep_bulk *b);
 
+/* ---- spin-orbit operator of the spinor filter (spinors/filterSpinors/) ----
+ * One neighbour-list entry, laid out as the reference's nlc_st
+ * (spinors/filterSpinors/fd.h:55-60), so its nlc arrays pass unchanged:
+ * grid index, the l = 1 harmonics Y10, Y11, Y1-1 (re, im), the
+ * Kleinman-Bylander radial factors, r, 1/r^2, r^2 and Vso(r). */
+typedef struct {
+  long jxyz;
+  double y10[2], y11[2], y1_1[2];
+  double Vs0G1, Vs0G_2;
+  double r, r2_1, r2, Vr;
+} sep_nlc;
+/* psinl = Vso psi for spinors of 2 ngrid complex values (interleaved re, im;
+ * the spin-up grid, then the spin-down grid).  natom atoms, each with nl[a]
+ * entries at nlc[a * nnlc].  flagkb = 0: the Gaussian form of
+ * filterSpinors/hamiltonian.c:81-190 with delta width sigma (sigma_1 =
+ * sqrt(1/2)/sigma as filterSpinors/init.c:96-97); flagkb = 1: the
+ * Kleinman-Bylander form of hamiltonian.c:193-401 with elkb = 2 natom
+ * energies (G1 block, then G_2).  dv = the volume element.  psinl is
+ * overwritten.  sep_spinor_vso takes host arrays and checks that every
+ * jxyz lies on the grid; sep_spinor_vso_dev takes device arrays (already
+ * checked) and runs on cuda_stream (a cudaStream_t; NULL = the legacy
+ * default stream). */
+int sep_spinor_vso(const double *psi, long ngrid, long natom, long nnlc, const sep_nlc *nlc,
+                   const long *nl, double sigma, double dv, int flagkb, const double *elkb,
+                   double *psinl);
+int sep_spinor_vso_dev(const double *psi, long ngrid, long natom, long nnlc,
+                       const sep_nlc *nlc, const long *nl, double sigma, double dv, int flagkb,
+                       const double *elkb, double *psinl, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,6 +36,40 @@ static inline void sep_shim_dsyev(const char *jobz, const char *uplo, long long 
   scipy_dsyev_64_(jobz, uplo, n, a, lda, w, work, lwork, info, 1, 1);
 }
 
+/* complex routines of spinors/filterSpinors (zgesvd_ in ortho.c:27, zheev_
+ * in Hmat.c:43); pointer arguments pass through untyped, as MKL's C
+ * prototypes accept the reference's own complex type */
+typedef struct {
+  double real, imag;
+} MKL_Complex16;
+void scipy_zgesvd_64_(const char *jobu, const char *jobvt, const long long *m,
+                      const long long *n, void *a, const long long *lda, double *s, void *u,
+                      const long long *ldu, void *vt, const long long *ldvt, void *work,
+                      const long long *lwork, double *rwork, long long *info, size_t l1,
+                      size_t l2);
+void scipy_zheev_64_(const char *jobz, const char *uplo, const long long *n, void *a,
+                     const long long *lda, double *w, void *work, const long long *lwork,
+                     double *rwork, long long *info, size_t l1, size_t l2);
+
+static inline void sep_shim_zgesvd(const char *jobu, const char *jobvt, const void *m,
+                                   const void *n, void *a, const void *lda, double *s, void *u,
+                                   const void *ldu, void *vt, const void *ldvt, void *work,
+                                   const void *lwork, double *rwork, void *info) {
+  scipy_zgesvd_64_(jobu, jobvt, (const long long *)m, (const long long *)n, a,
+                   (const long long *)lda, s, u, (const long long *)ldu, vt,
+                   (const long long *)ldvt, work, (const long long *)lwork, rwork,
+                   (long long *)info, 1, 1);
+}
+
+static inline void sep_shim_zheev(const char *jobz, const char *uplo, const void *n, void *a,
+                                  const void *lda, double *w, void *work, const void *lwork,
+                                  double *rwork, void *info) {
+  scipy_zheev_64_(jobz, uplo, (const long long *)n, a, (const long long *)lda, w, work,
+                  (const long long *)lwork, rwork, (long long *)info, 1, 1);
+}
+
+#define zgesvd_ sep_shim_zgesvd
+#define zheev_ sep_shim_zheev
 #define dgesvd_ sep_shim_dgesvd
 #define dsyev_ sep_shim_dsyev
 #define mkl_set_dynamic(x) ((void)(x))

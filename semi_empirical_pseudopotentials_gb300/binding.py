@@ -119,6 +119,10 @@ def lib():
         L.sep_bulk_solver_path.argtypes = [vp, ip]
         L.sep_bulk_set_solver.argtypes = [vp, C.c_int]
         L.sep_bulk_destroy.argtypes = [vp]
+        L.sep_spinor_vso.argtypes = [dp, C.c_long, C.c_long, C.c_long, vp, lp, C.c_double,
+                                     C.c_double, C.c_int, dp, dp]
+        L.sep_spinor_vso_dev.argtypes = [vp, C.c_long, C.c_long, C.c_long, vp, vp, C.c_double,
+                                         C.c_double, C.c_int, vp, vp, vp]
         _lib = L
     return _lib
 

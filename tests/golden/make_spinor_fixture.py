@@ -1,0 +1,108 @@
+"""Golden vectors for the spin-orbit operator of the spinor filter
+(spinors/filterSpinors/), from the reference's own code.
+
+Run in a container that has the reference checkout (not on a GPU machine), after
+`python oracle/build_oracle.py` has compiled oracle/_ref/libspinorref.so from
+the reference's sources:
+
+    python tests/golden/make_spinor_fixture.py
+
+On a 20 x 18 x 16 grid (0.55 bohr) with three atoms it calls the
+reference's init_list (filterSpinors/init.c:114-181) for the neighbour
+lists, fills the Kleinman-Bylander fields (Vs0G1, Vs0G_2, Elkb; made by
+init_kb in a full run) with seeded values, and applies nonlocal_potential
+(Gaussian form, hamiltonian.c:81-190) and nonlocal_potential_kb
+(hamiltonian.c:193-401) to a seeded random spinor.  The arrays go to
+tests/golden/spinor_vso.npz.
+"""
+import ctypes as C
+import os
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "..", "..", "oracle", "_ref", "libspinorref.so")
+
+
+class LongSt(C.Structure):   # filterSpinors/fd.h:31-40
+    _fields_ = [(n, C.c_long) for n in (
+        "natom", "lumo", "homo", "flaghomo", "nsemicond", "ms", "ns", "nc", "npot", "mstot",
+        "mstotngrid", "nspinngrid", "nx", "ny", "nz", "ngrid", "nspin", "nnlc", "natomtype",
+        "nthreads", "flagkb")] + [("nx_1", C.c_double), ("ny_1", C.c_double),
+                                  ("nz_1", C.c_double)]
+
+
+class ParSt(C.Structure):    # filterSpinors/fd.h:24-29
+    _fields_ = [(n, C.c_double) for n in (
+        "dx", "dy", "dz", "dr", "dkx", "dky", "dkz", "dv", "dt", "xmin", "xmax", "ymin", "ymax",
+        "zmin", "zmax", "Vmin", "Vmax", "dE", "dE_1", "Elmin", "Elmax", "Ekinmax", "Rnlcut2",
+        "sigma", "sigma_1")]
+
+
+class AtmSt(C.Structure):    # filterSpinors/fd.h:46-50
+    _fields_ = [("natyp", C.c_long), ("atyp", C.c_char * 3), ("Vso", C.c_double),
+                ("initE", C.c_double)]
+
+
+def main():
+    from oracle.spinor_oracle import NLC_DTYPE
+
+    L = C.CDLL(os.path.abspath(LIB))
+    nx, ny, nz, h = 20, 18, 16, 0.55
+    ngrid = nx * ny * nz
+    vx = -0.5 * nx * h + h * np.arange(nx)
+    vy = -0.5 * ny * h + h * np.arange(ny)
+    vz = -0.5 * nz * h + h * np.arange(nz)
+    rxyz = np.array([[0.31, -0.42, 0.17], [-1.93, 1.12, -0.86], [1.71, 1.29, 1.03]])
+    vso = np.array([0.0813, -0.0457, 0.1221])
+    nat = len(rxyz)
+    rnlcut2 = 0.49 * 6.0 * np.log(10.0)              # init.c:99
+    nnlc = 800                                      # > the ~450 points per atom
+    ist = LongSt(natom=nat, nsemicond=nat, nx=nx, ny=ny, nz=nz, ngrid=ngrid, nspin=2,
+                 nspinngrid=2 * ngrid, nnlc=nnlc, nthreads=1)
+    par = ParSt(dx=h, dy=h, dz=h, dv=h ** 3, Rnlcut2=rnlcut2, sigma=h,
+                sigma_1=np.sqrt(0.5) / h)            # init.c:96-97
+    atm = (AtmSt * nat)()
+    for a in range(nat):
+        atm[a].Vso = vso[a]
+    nlc = np.zeros(nat * nnlc, dtype=NLC_DTYPE)
+    nl = np.zeros(nat, dtype=np.int64)
+    dp = C.POINTER(C.c_double)
+    rx, ry, rz = (np.ascontiguousarray(rxyz[:, k]) for k in range(3))
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as tmp:      # init_list writes list.dat
+        os.chdir(tmp)
+        try:
+            L.init_list(nlc.ctypes.data_as(C.c_void_p), nl.ctypes.data_as(C.c_void_p),
+                        vx.ctypes.data_as(dp), vy.ctypes.data_as(dp), vz.ctypes.data_as(dp),
+                        rx.ctypes.data_as(dp), ry.ctypes.data_as(dp), rz.ctypes.data_as(dp),
+                        atm, par, ist)
+        finally:
+            os.chdir(cwd)
+    rng = np.random.default_rng(2026)
+    nlc["Vs0G1"] = rng.normal(size=nlc.shape)
+    nlc["Vs0G_2"] = rng.normal(size=nlc.shape)
+    elkb = rng.uniform(0.5, 2.0, size=2 * nat)
+    psi = rng.normal(size=2 * ngrid) + 1j * rng.normal(size=2 * ngrid)
+    out_g = np.zeros(2 * ngrid, dtype=np.complex128)
+    out_k = np.zeros(2 * ngrid, dtype=np.complex128)
+    L.nonlocal_potential(out_g.ctypes.data_as(C.c_void_p), psi.ctypes.data_as(C.c_void_p), ist,
+                         par, nlc.ctypes.data_as(C.c_void_p), nl.ctypes.data_as(C.c_void_p))
+    L.nonlocal_potential_kb(out_k.ctypes.data_as(C.c_void_p), psi.ctypes.data_as(C.c_void_p),
+                            ist, par, nlc.ctypes.data_as(C.c_void_p),
+                            nl.ctypes.data_as(C.c_void_p), elkb.ctypes.data_as(dp))
+    width = int(nl.max())                            # entries past nl[a] are unused
+    keep = nlc.reshape(nat, nnlc)[:, :width].copy()
+    np.savez_compressed(os.path.join(HERE, "spinor_vso.npz"), dims=np.array([nx, ny, nz]), h=h,
+                        vx=vx, vy=vy, vz=vz, rxyz=rxyz, vso=vso, rnlcut2=rnlcut2, nnlc=width,
+                        nlc=keep.view(np.uint8).reshape(nat, width, NLC_DTYPE.itemsize), nl=nl,
+                        elkb=elkb, psi=psi, vso_gauss=out_g, vso_kb=out_k)
+    print("nl", nl, "|gauss|", np.abs(out_g).max(), "|kb|", np.abs(out_k).max())
+
+
+if __name__ == "__main__":
+    import sys
+
+    sys.path.insert(0, os.path.join(HERE, "..", ".."))
+    main()
