@@ -404,6 +404,19 @@ int sep_spinor_vso(const double *psi, long ngrid, long natom, long nnlc, const s
 int sep_spinor_vso_dev(const double *psi, long ngrid, long natom, long nnlc,
                        const sep_nlc *nlc, const long *nl, double sigma, double dv, int flagkb,
                        const double *elkb, double *psinl, void *cuda_stream);
+/* The neighbour lists of filterSpinors/init.c:114-181 (init_list), entry
+ * for entry: for atom a at rxyz[3a..3a+2] (bohr) the points of the grid
+ * vx[nx] x vy[ny] x vz[nz] (x fastest) with squared distance below rnlcut2,
+ * Vr = vso[a] exp(-r^2 / 0.49), the harmonics and r, 1/r^2, r^2; Vs0G1 and
+ * Vs0G_2 are left 0 (filterSpinors/init.c:183+ fills them for the
+ * Kleinman-Bylander form).  nl[a] receives the count.  nlc == NULL: counts
+ * only (to size nnlc); else nlc holds natom x nnlc entries and a count above
+ * nnlc is SEP_ERR_ARG (the reference would write past its array).  Host
+ * only; each atom visits only the box of grid lines within its radius. */
+int sep_spinor_neighbour_lists(long nx, long ny, long nz, const double *vx, const double *vy,
+                               const double *vz, long natom, const double *rxyz,
+                               const double *vso, double rnlcut2, long nnlc, sep_nlc *nlc,
+                               long *nl);
 
 #ifdef __cplusplus
 }

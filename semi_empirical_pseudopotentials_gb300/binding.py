@@ -121,6 +121,8 @@ def lib():
         L.sep_bulk_destroy.argtypes = [vp]
         L.sep_spinor_vso.argtypes = [dp, C.c_long, C.c_long, C.c_long, vp, lp, C.c_double,
                                      C.c_double, C.c_int, dp, dp]
+        L.sep_spinor_neighbour_lists.argtypes = [C.c_long, C.c_long, C.c_long, dp, dp, dp,
+                                                 C.c_long, dp, dp, C.c_double, C.c_long, vp, lp]
         L.sep_spinor_vso_dev.argtypes = [vp, C.c_long, C.c_long, C.c_long, vp, vp, C.c_double,
                                          C.c_double, C.c_int, vp, vp, vp]
         _lib = L

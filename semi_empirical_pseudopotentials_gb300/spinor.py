@@ -7,6 +7,8 @@ reference's nlc_st (NLC_DTYPE, filterSpinors/fd.h:55-60), natom x nnlc, of
 which nl[a] entries are used for atom a; the reference's own nlc arrays have
 this layout.
 
+* ``neighbour_lists(vx, vy, vz, rxyz, vso, rnlcut2)``: the lists of
+  filterSpinors/init.c:114-181 (host code of the library);
 * ``nonlocal_potential(psi, nlc, nl, sigma, dv)``: the Gaussian form,
   filterSpinors/hamiltonian.c:81-190;
 * ``nonlocal_potential_kb(psi, nlc, nl, elkb, dv)``: the Kleinman-Bylander
@@ -21,6 +23,32 @@ from .binding import _check, lib
 NLC_DTYPE = np.dtype([("jxyz", "<i8"), ("y10", "<c16"), ("y11", "<c16"), ("y1_1", "<c16"),
                       ("Vs0G1", "<f8"), ("Vs0G_2", "<f8"), ("r", "<f8"), ("r2_1", "<f8"),
                       ("r2", "<f8"), ("Vr", "<f8")])
+
+
+def neighbour_lists(vx, vy, vz, rxyz, vso, rnlcut2, nnlc=None):
+    """(nlc natom x nnlc, nl) for atoms at rxyz with spin-orbit strengths vso
+    on the grid vx x vy x vz (filterSpinors/init.c:114-181).  nnlc defaults
+    to the largest count."""
+    vx, vy, vz = (np.ascontiguousarray(v, dtype=np.float64) for v in (vx, vy, vz))
+    rxyz = np.ascontiguousarray(rxyz, dtype=np.float64).reshape(-1, 3)
+    vso = np.ascontiguousarray(vso, dtype=np.float64).ravel()
+    natom = len(rxyz)
+    if vso.shape != (natom,):
+        raise ValueError("vso has one entry per atom")
+    dp = C.POINTER(C.c_double)
+    nl = np.zeros(natom, dtype=np.int64)
+    L = lib()
+    args = (len(vx), len(vy), len(vz), vx.ctypes.data_as(dp), vy.ctypes.data_as(dp),
+            vz.ctypes.data_as(dp), natom, rxyz.ctypes.data_as(dp), vso.ctypes.data_as(dp),
+            float(rnlcut2))
+    lp = C.POINTER(C.c_long)
+    if nnlc is None:
+        _check(L.sep_spinor_neighbour_lists(*args, 0, None, nl.ctypes.data_as(lp)))
+        nnlc = int(nl.max()) if natom else 0
+    nlc = np.zeros((natom, int(nnlc)), dtype=NLC_DTYPE)
+    _check(L.sep_spinor_neighbour_lists(*args, int(nnlc), nlc.ctypes.data_as(C.c_void_p),
+                                        nl.ctypes.data_as(lp)))
+    return nlc, nl
 
 
 def _apply(psi, nlc, nl, sigma, dv, flagkb, elkb):

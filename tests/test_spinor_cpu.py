@@ -31,6 +31,18 @@ def test_neighbour_lists_match_reference(golden):
     assert np.allclose(nlc["Vr"], ref["Vr"], rtol=4e-16, atol=0)
 
 
+def test_library_neighbour_lists_match_reference(golden):
+    g, ref = load(golden)
+    nlc, nl = spinor.neighbour_lists(g["vx"], g["vy"], g["vz"], g["rxyz"], g["vso"],
+                                     float(g["rnlcut2"]))
+    assert np.array_equal(nl, g["nl"]) and nlc.shape == ref.shape
+    for f in ("jxyz", "y10", "y11", "y1_1", "r", "r2_1", "r2", "Vr"):
+        assert np.array_equal(nlc[f], ref[f]), f
+    with pytest.raises(SepError, match="nnlc is too small"):
+        spinor.neighbour_lists(g["vx"], g["vy"], g["vz"], g["rxyz"], g["vso"],
+                               float(g["rnlcut2"]), nnlc=int(g["nl"].max()) - 1)
+
+
 @pytest.mark.parametrize("form", ["gauss", "kb"])
 def test_operator_matches_reference(golden, form):
     g, nlc = load(golden)
