@@ -1,12 +1,15 @@
-"""CPU restatement of the spin-orbit part of the reference's spinor filter
-(spinors/filterSpinors/): TEST INFRASTRUCTURE ONLY.
+"""CPU restatement of the reference's spinor filter (spinors/filterSpinors/):
+neighbour lists, the spin-orbit operator in both forms, the spinor
+Hamiltonian and the Newton filter with complex coefficients.
+TEST INFRASTRUCTURE ONLY.
 
 Only tests/ and bench.py's CPU-baseline leg use this module, as the checker;
-the product applies the operator on the GPU (csrc/sep_spinor.cu).
+the product applies the spin-orbit operator on the GPU (csrc/sep_spinor.cu).
 
-Pinned against the reference's own init_list, nonlocal_potential and
-nonlocal_potential_kb, compiled from its sources by oracle/Makefile.ref
-(tests/golden/spinor_vso.npz, made by tests/golden/make_spinor_fixture.py).
+Pinned against the reference's own init_list, nonlocal_potential,
+nonlocal_potential_kb, hamiltonian and filter, compiled from its sources by
+oracle/Makefile.ref (tests/golden/spinor_vso.npz, made by
+tests/golden/make_spinor_fixture.py).
 
 Spinors are 2 ngrid complex values: the spin-up grid, then the spin-down
 grid (filterSpinors/hamiltonian.c:38-44).  The neighbour lists are
@@ -133,4 +136,43 @@ def vso_kb(psi, nlc, nl, elkb, dv, ngrid):
                            + s3 * g1 * (P("G1", "10", "up") * y10)
                            - 1.0 / 3.0 * g1 * (P("G1", "10", "dn") * y10)
                            - 2.0 / 3.0 * g1 * (P("G1", "11", "dn") * y11))
+    return out
+
+
+def kinetic(x, ksqr, dims):
+    """T x = IFFT(ksqr FFT x) on one complex grid (x fastest); ksqr carries
+    the 1/N of the unnormalised inverse, filterSpinors/hamiltonian.c:51-76."""
+    nx, ny, nz = dims
+    f = np.fft.fftn(np.asarray(x).reshape(nz, ny, nx)) * np.asarray(ksqr).reshape(nz, ny, nx)
+    return (np.fft.ifftn(f) * (nx * ny * nz)).ravel()
+
+
+def hamiltonian(psi, potl, ksqr, dims, nlc, nl, sigma, dv, flagkb=0, elkb=None):
+    """H psi = T psi + V psi + Vso psi on a spinor (up grid, then down grid),
+    filterSpinors/hamiltonian.c:8-46."""
+    n = int(np.prod(dims))
+    psi = np.asarray(psi, dtype=np.complex128)
+    nlp = (vso_kb(psi, nlc, nl, elkb, dv, n) if flagkb else vso_gauss(psi, nlc, nl, sigma, dv, n))
+    out = np.empty_like(psi)
+    for s in (0, 1):
+        part = psi[s * n:(s + 1) * n]
+        out[s * n:(s + 1) * n] = kinetic(part, ksqr, dims) + (potl * part + nlp[s * n:(s + 1) * n])
+    return out
+
+
+def hnorm(psi, zm1, dE_1, vmin, *hargs, **hkw):
+    """(H - z) psi in the filter's scaled form, filterSpinors/hnorm.c:5-17."""
+    return dE_1 * hamiltonian(psi, *hargs, **hkw) - (2.0 + zm1 + vmin * dE_1) * psi
+
+
+def newton_filter(start, an, zn, dE_1, vmin, *hargs, **hkw):
+    """psims[e] = sum_j an[e, j] psi_j with psi_0 = start and
+    psi_j = (H - z_{j-1}) psi_{j-1}; complex coefficients,
+    filterSpinors/filter.c:48-80."""
+    an = np.asarray(an)
+    psi = np.asarray(start, dtype=np.complex128).copy()
+    out = an[:, :1] * psi[None, :]
+    for j in range(1, an.shape[1]):
+        psi = hnorm(psi, zn[j - 1], dE_1, vmin, *hargs, **hkw)
+        out += an[:, j:j + 1] * psi[None, :]
     return out

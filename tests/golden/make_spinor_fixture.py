@@ -7,13 +7,16 @@ the reference's sources:
 
     python tests/golden/make_spinor_fixture.py
 
-On a 20 x 18 x 16 grid (0.55 bohr) with three atoms it calls the
+On a 16 x 16 x 14 grid (0.6 bohr) with three atoms it calls the
 reference's init_list (filterSpinors/init.c:114-181) for the neighbour
 lists, fills the Kleinman-Bylander fields (Vs0G1, Vs0G_2, Elkb; made by
 init_kb in a full run) with seeded values, and applies nonlocal_potential
 (Gaussian form, hamiltonian.c:81-190) and nonlocal_potential_kb
-(hamiltonian.c:193-401) to a seeded random spinor.  The arrays go to
-tests/golden/spinor_vso.npz.
+(hamiltonian.c:193-401) to a seeded random spinor.  It then applies the
+whole spinor hamiltonian() (hamiltonian.c:8-46) in both forms and runs a
+6-step Newton filter() (filter.c:48-80) with complex coefficients for two
+targets, with a local potential of Gaussian wells at the atoms.  The arrays
+go to tests/golden/spinor_vso.npz.
 """
 import ctypes as C
 import os
@@ -49,7 +52,7 @@ def main():
     from oracle.spinor_oracle import NLC_DTYPE
 
     L = C.CDLL(os.path.abspath(LIB))
-    nx, ny, nz, h = 20, 18, 16, 0.55
+    nx, ny, nz, h = 16, 16, 14, 0.6
     ngrid = nx * ny * nz
     vx = -0.5 * nx * h + h * np.arange(nx)
     vy = -0.5 * ny * h + h * np.arange(ny)
@@ -58,7 +61,7 @@ def main():
     vso = np.array([0.0813, -0.0457, 0.1221])
     nat = len(rxyz)
     rnlcut2 = 0.49 * 6.0 * np.log(10.0)              # init.c:99
-    nnlc = 800                                      # > the ~450 points per atom
+    nnlc = 600                                      # > the ~340 points per atom
     ist = LongSt(natom=nat, nsemicond=nat, nx=nx, ny=ny, nz=nz, ngrid=ngrid, nspin=2,
                  nspinngrid=2 * ngrid, nnlc=nnlc, nthreads=1)
     par = ParSt(dx=h, dy=h, dz=h, dv=h ** 3, Rnlcut2=rnlcut2, sigma=h,
@@ -92,13 +95,72 @@ def main():
     L.nonlocal_potential_kb(out_k.ctypes.data_as(C.c_void_p), psi.ctypes.data_as(C.c_void_p),
                             ist, par, nlc.ctypes.data_as(C.c_void_p),
                             nl.ctypes.data_as(C.c_void_p), elkb.ctypes.data_as(dp))
+    # the whole spinor Hamiltonian (filterSpinors/hamiltonian.c:8-46) in both
+    # spin-orbit forms, and a short Newton filter (filter.c:48-80), through
+    # the reference's own routines with FFT plans of the oracle's shim
+    import semi_empirical_pseudopotentials_gb300 as sep
+
+    ksqr = sep.ksqr((nx, ny, nz), (h, h, h), ekinmax=20.0)   # init.c:23, 442-460
+    zz, yy, xx = np.meshgrid(vz, vy, vx, indexing="ij")
+    potl = np.zeros(ngrid)
+    for a in range(nat):
+        d2 = (xx - rxyz[a, 0]) ** 2 + (yy - rxyz[a, 1]) ** 2 + (zz - rxyz[a, 2]) ** 2
+        potl -= 0.4 * np.exp(-0.5 * d2).ravel()
+    L.fftw_malloc.restype = C.c_void_p
+    L.fftw_plan_dft_3d.restype = C.c_void_p
+    buf = C.c_void_p(L.fftw_malloc(C.c_size_t(16 * ngrid)))
+    planfw = C.c_void_p(L.fftw_plan_dft_3d(nz, ny, nx, buf, buf, -1, 0))
+    planbw = C.c_void_p(L.fftw_plan_dft_3d(nz, ny, nx, buf, buf, 1, 0))
+    vp = C.c_void_p
+    hpsi = {}
+    for flag, name in ((0, "gauss"), (1, "kb")):
+        ist.flagkb = flag
+        phi = psi.copy()
+        scratch = np.zeros_like(psi)
+        L.hamiltonian(phi.ctypes.data_as(vp), scratch.ctypes.data_as(vp), potl.ctypes.data_as(dp),
+                      ksqr.ctypes.data_as(dp), ist, par, nlc.ctypes.data_as(vp),
+                      nl.ctypes.data_as(vp), elkb.ctypes.data_as(dp), planfw, planbw, buf)
+        hpsi[name] = phi
+    ms, nc = 2, 6
+    an = rng.normal(size=ms * nc) + 1j * rng.normal(size=ms * nc)
+    zn = rng.uniform(-2.0, 2.0, size=nc)
+    par.dE_1, par.Vmin = 4.0 / 3.5, -0.45
+    ist.flagkb, ist.ms, ist.nc = 0, ms, nc
+    psin = psi.copy()
+    psim1 = np.zeros_like(psi)
+    psims = np.zeros(ms * 2 * ngrid, dtype=np.complex128)
+    with tempfile.TemporaryDirectory() as tmp:      # filter writes prop<tid>.dat
+        os.chdir(tmp)
+        try:
+            L.filter(psin.ctypes.data_as(vp), psim1.ctypes.data_as(vp), psims.ctypes.data_as(vp),
+                     potl.ctypes.data_as(dp), ksqr.ctypes.data_as(dp), par, nlc.ctypes.data_as(vp),
+                     nl.ctypes.data_as(vp), elkb.ctypes.data_as(dp), an.ctypes.data_as(vp),
+                     zn.ctypes.data_as(dp), ist, planfw, planbw, buf, C.c_long(0), C.c_long(0))
+        finally:
+            os.chdir(cwd)
+    # Vso psi is zero away from the atoms: kept where it is not; the other
+    # outputs as 1024 seeded samples plus the sum and the sum of squares
+    outputs = {}
+    for name, arr in (("vso_gauss", out_g), ("vso_kb", out_k)):
+        nz_idx = np.flatnonzero(arr)
+        outputs[name + "_idx"], outputs[name + "_val"] = nz_idx, arr[nz_idx]
+    pick = np.sort(np.random.default_rng(99).choice(2 * ngrid, 1024, replace=False))
+    for name, arr in (("h_gauss", hpsi["gauss"]), ("h_kb", hpsi["kb"]),
+                      ("filter_out", psims.reshape(ms, 2 * ngrid))):
+        flat = arr.reshape(-1, 2 * ngrid)
+        outputs[name + "_sample"] = flat[:, pick]
+        outputs[name + "_sum"] = flat.sum(axis=1)
+        outputs[name + "_sumsq"] = (np.abs(flat) ** 2).sum(axis=1)
+    outputs["sample_idx"] = pick
     width = int(nl.max())                            # entries past nl[a] are unused
     keep = nlc.reshape(nat, nnlc)[:, :width].copy()
     np.savez_compressed(os.path.join(HERE, "spinor_vso.npz"), dims=np.array([nx, ny, nz]), h=h,
                         vx=vx, vy=vy, vz=vz, rxyz=rxyz, vso=vso, rnlcut2=rnlcut2, nnlc=width,
                         nlc=keep.view(np.uint8).reshape(nat, width, NLC_DTYPE.itemsize), nl=nl,
-                        elkb=elkb, psi=psi, vso_gauss=out_g, vso_kb=out_k)
-    print("nl", nl, "|gauss|", np.abs(out_g).max(), "|kb|", np.abs(out_k).max())
+                        elkb=elkb, psi=psi, ksqr=ksqr, potl=potl, an=an.reshape(ms, nc), zn=zn,
+                        dE_1=par.dE_1, vmin=par.Vmin, **outputs)
+    print("nl", nl, "|gauss|", np.abs(out_g).max(), "|kb|", np.abs(out_k).max(),
+          "|H psi|", np.abs(hpsi["gauss"]).max(), "|filter|", np.abs(psims).max())
 
 
 if __name__ == "__main__":

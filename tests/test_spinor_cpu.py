@@ -16,6 +16,23 @@ def load(golden):
     return g, nlc
 
 
+def dense(g, name):
+    """The reference's Vso psi: zero away from its stored entries."""
+    out = np.zeros(2 * int(np.prod(g["dims"])), dtype=np.complex128)
+    out[g[name + "_idx"]] = g[name + "_val"]
+    return out
+
+
+def check_sampled(g, name, got):
+    """got (rows x 2N) against the stored samples, sums and sums of squares."""
+    got = np.asarray(got).reshape(-1, 2 * int(np.prod(g["dims"])))
+    ref = g[name + "_sample"].reshape(got.shape[0], -1)
+    scale = np.abs(ref).max()
+    assert np.abs(got[:, g["sample_idx"]] - ref).max() <= 1e-12 * scale
+    assert np.allclose(got.sum(axis=1), g[name + "_sum"], rtol=1e-11, atol=1e-12 * scale)
+    assert np.allclose((np.abs(got) ** 2).sum(axis=1), g[name + "_sumsq"], rtol=1e-11, atol=0)
+
+
 def test_layouts_match():
     assert so.NLC_DTYPE == spinor.NLC_DTYPE and so.NLC_DTYPE.itemsize == 104
 
@@ -52,8 +69,27 @@ def test_operator_matches_reference(golden, form):
         got = so.vso_gauss(g["psi"], nlc, g["nl"], h, h ** 3, n)
     else:
         got = so.vso_kb(g["psi"], nlc, g["nl"], g["elkb"], h ** 3, n)
-    ref = g["vso_" + form]
+    ref = dense(g, "vso_" + form)
     assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("form", ["gauss", "kb"])
+def test_hamiltonian_matches_reference(golden, form):
+    g, nlc = load(golden)
+    dims = tuple(int(v) for v in g["dims"])
+    h = float(g["h"])
+    got = so.hamiltonian(g["psi"], g["potl"], g["ksqr"], dims, nlc, g["nl"], h, h ** 3,
+                         flagkb=int(form == "kb"), elkb=g["elkb"])
+    check_sampled(g, "h_" + form, got)
+
+
+def test_newton_filter_matches_reference(golden):
+    g, nlc = load(golden)
+    dims = tuple(int(v) for v in g["dims"])
+    h = float(g["h"])
+    got = so.newton_filter(g["psi"], g["an"], g["zn"], float(g["dE_1"]), float(g["vmin"]),
+                           g["potl"], g["ksqr"], dims, nlc, g["nl"], h, h ** 3)
+    check_sampled(g, "filter_out", got)
 
 
 def test_library_rejects_entries_off_the_grid(golden):
