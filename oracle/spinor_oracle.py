@@ -176,3 +176,71 @@ def newton_filter(start, an, zn, dE_1, vmin, *hargs, **hkw):
         psi = hnorm(psi, zn[j - 1], dE_1, vmin, *hargs, **hkw)
         out += an[:, j:j + 1] * psi[None, :]
     return out
+
+
+def _normalize(x, dv):
+    """norm.c:27-44: x / sqrt(dv sum |x|^2)."""
+    return x / np.sqrt(np.sum(x.real ** 2 + x.imag ** 2) * dv)
+
+
+def energy(psi, dv, *hargs, **hkw):
+    """Re <psi|H|psi> dv, filterSpinors/energy.c:5-20."""
+    hp = hamiltonian(psi, *hargs, **hkw)
+    return float(np.sum(psi.real * hp.real + psi.imag * hp.imag) * dv)
+
+
+def energy_range(starts, dv, *hargs, tau=0.025, **hkw):
+    """(Vmin, dE) of filterSpinors/energy.c:49-109: Emin by the damped
+    iteration phi <- psi - tau H psi, Emax by power iteration, each to a
+    relative change of 1e-6 or 500 steps; Emax * 1.2, Emin - 0.2 |Emin|.
+    starts = the four normalised component grids that init_psi draws there
+    (two spinors: Emin's, then Emax's)."""
+    n = len(starts[0])
+    phi = np.concatenate([starts[0], starts[1]]).astype(np.complex128)
+    emin, old, i = 0.1, 0.0, 0
+    while abs((emin - old) / emin) > 1.0e-6 and i < 500:
+        psi = phi
+        phi = _normalize(psi - tau * hamiltonian(psi, *hargs, **hkw), dv)
+        old, emin = emin, energy(phi, dv, *hargs, **hkw)
+        i += 1
+    psi = np.concatenate([starts[2], starts[3]]).astype(np.complex128)
+    emax, old, i = 0.1, 0.0, 0
+    while abs((emax - old) / emax) > 1.0e-6 and i < 500:
+        psi = _normalize(hamiltonian(psi, *hargs, **hkw), dv)
+        old, emax = emax, energy(psi, dv, *hargs, **hkw)
+        i += 1
+    emax *= 1.2
+    emin -= 0.2 * abs(emin)
+    return emin, emax - emin
+
+
+def pipeline(spinors, an, zn, dE_1, vmin, dv, *hargs, **hkw):
+    """Filter every start spinor for all targets, normalise, orthogonalise
+    (SVD, keep S_i / S_0 >= 1e-10), Rayleigh-Ritz and sigma:
+    filterSpinors/main.c:92-131 with filter.c, norm.c:47-60, ortho.c:5-40,
+    Hmat.c:5-75, energy.c:114-145.  Returns (eval, sigma)."""
+    blocks = []
+    for s in spinors:
+        out = newton_filter(s, an, zn, dE_1, vmin, *hargs, **hkw)
+        blocks.extend(_normalize(row, dv) for row in out)
+    psi = np.array(blocks)                               # mstot x 2N
+    u, sv, _ = np.linalg.svd(psi.T, full_matrices=False)
+    keep = len(sv)
+    for i in range(len(sv)):
+        if sv[i] / sv[0] < 1.0e-10:
+            keep = i
+            break
+    basis = np.array([_normalize(u[:, i], dv) for i in range(keep)])
+    hb = np.array([hamiltonian(b, *hargs, **hkw) for b in basis])
+    hm = (np.conj(basis) @ hb.T) * dv                    # <b_i|H|b_j>
+    ev, vec = np.linalg.eigh(0.5 * (hm + np.conj(hm.T)))
+    rot = vec.T @ basis
+    rot = np.array([_normalize(r, dv) for r in rot])
+    sig = []
+    for r in rot:
+        h1 = hamiltonian(r, *hargs, **hkw)
+        h2 = hamiltonian(h1, *hargs, **hkw)
+        e1 = np.sum(r.real * h1.real + r.imag * h1.imag) * dv
+        e2 = np.sum(r.real * h2.real + r.imag * h2.imag) * dv
+        sig.append(np.sqrt(abs(e2 - e1 * e1)))
+    return ev, np.array(sig)

@@ -152,6 +152,71 @@ def main():
         outputs[name + "_sum"] = flat.sum(axis=1)
         outputs[name + "_sumsq"] = (np.abs(flat) ** 2).sum(axis=1)
     outputs["sample_idx"] = pick
+    # the reference's whole spinor program on this system (main.c:92-131 with
+    # its energy range, coefficients, start states, filtering, portho, Hmat
+    # and calc_sigma_E), with a fixed start seed in place of -random()
+    ist.flagkb, ist.ms, ist.ns, ist.nc = 0, 2, 2, 64
+    ist.mstot = ist.ms * ist.ns
+    scratch_a = np.zeros(2 * ngrid, dtype=np.complex128)
+    scratch_b = np.zeros(2 * ngrid, dtype=np.complex128)
+    el = np.array([-0.36, -0.28])
+    with tempfile.TemporaryDirectory() as tmp:       # the stages write log files
+        os.chdir(tmp)
+        try:
+            L.get_energy_range(scratch_a.ctypes.data_as(vp), scratch_b.ctypes.data_as(vp),
+                               potl.ctypes.data_as(dp), vx.ctypes.data_as(dp),
+                               vy.ctypes.data_as(dp), vz.ctypes.data_as(dp),
+                               ksqr.ctypes.data_as(dp), ist, C.byref(par),
+                               nlc.ctypes.data_as(vp), nl.ctypes.data_as(vp),
+                               elkb.ctypes.data_as(dp), planfw, planbw, buf)
+            par.dt = (ist.nc / (2.5 * par.dE)) ** 2          # main.c:84
+            an_p = np.zeros(ist.nc * ist.ms, dtype=np.complex128)
+            zn_p = np.zeros(ist.nc)
+            L.coefficient(an_p.ctypes.data_as(vp), zn_p.ctypes.data_as(dp), el.ctypes.data_as(dp),
+                          par, ist)
+            seed = -20261203
+            idum = C.c_long(seed)
+            psitot = np.zeros(ist.mstot * 2 * ngrid, dtype=np.complex128)
+            start = np.zeros(2 * ngrid, dtype=np.complex128)
+            for jns in range(ist.ns):
+                for ispn in range(2):
+                    L.init_psi(C.c_void_p(start.ctypes.data + 16 * ispn * ngrid), ist, par,
+                               C.byref(idum))
+                for jms in range(ist.ms):
+                    o = (jns * ist.ms + jms) * 2 * ngrid
+                    psitot[o:o + 2 * ngrid] = start
+            for jns in range(ist.ns):
+                L.filtering(C.c_void_p(psitot.ctypes.data + 16 * jns * ist.ms * 2 * ngrid),
+                            potl.ctypes.data_as(dp), ksqr.ctypes.data_as(dp),
+                            an_p.ctypes.data_as(vp), zn_p.ctypes.data_as(dp),
+                            el.ctypes.data_as(dp), ist, par, nlc.ctypes.data_as(vp),
+                            nl.ctypes.data_as(vp), elkb.ctypes.data_as(dp), C.c_long(0),
+                            C.c_long(jns))
+            L.portho.restype = C.c_long
+            ist.mstot = L.portho(psitot.ctypes.data_as(vp), C.c_double(par.dv), ist)
+            L.normalize_all(psitot.ctypes.data_as(vp), C.c_double(par.dv), C.c_long(ist.mstot),
+                            C.c_long(2 * ngrid), C.c_long(1))
+            evals = np.zeros(ist.mstot)
+            L.Hmat(scratch_a.ctypes.data_as(vp), scratch_b.ctypes.data_as(vp),
+                   psitot.ctypes.data_as(vp), potl.ctypes.data_as(dp), ksqr.ctypes.data_as(dp),
+                   evals.ctypes.data_as(dp), ist, par, nlc.ctypes.data_as(vp),
+                   nl.ctypes.data_as(vp), elkb.ctypes.data_as(dp), planfw, planbw, buf)
+            L.normalize_all(psitot.ctypes.data_as(vp), C.c_double(par.dv), C.c_long(ist.mstot),
+                            C.c_long(2 * ngrid), C.c_long(1))
+            sige = np.zeros(ist.mstot)
+            L.calc_sigma_E(scratch_a.ctypes.data_as(vp), scratch_b.ctypes.data_as(vp),
+                           psitot.ctypes.data_as(vp), potl.ctypes.data_as(dp),
+                           ksqr.ctypes.data_as(dp), sige.ctypes.data_as(dp), ist, par,
+                           nlc.ctypes.data_as(vp), nl.ctypes.data_as(vp),
+                           elkb.ctypes.data_as(dp), planfw, planbw, buf)
+        finally:
+            os.chdir(cwd)
+    outputs["run_seed"], outputs["run_el"], outputs["run_nc"] = seed, el, ist.nc
+    outputs["run_ns"], outputs["run_ms"] = ist.ns, ist.ms
+    outputs["run_vmin"], outputs["run_dE"] = par.Vmin, par.dE
+    outputs["run_an"], outputs["run_zn"] = an_p.reshape(ist.ms, ist.nc), zn_p
+    outputs["run_eval"], outputs["run_sigma"], outputs["run_mkept"] = evals, sige, ist.mstot
+    print("energy range", par.Vmin, par.dE, "eval", evals, "sigma", sige)
     width = int(nl.max())                            # entries past nl[a] are unused
     keep = nlc.reshape(nat, nnlc)[:, :width].copy()
     np.savez_compressed(os.path.join(HERE, "spinor_vso.npz"), dims=np.array([nx, ny, nz]), h=h,

@@ -100,3 +100,35 @@ def test_library_rejects_entries_off_the_grid(golden):
         spinor.nonlocal_potential(g["psi"], bad, g["nl"], float(g["h"]), float(g["h"]) ** 3)
     with pytest.raises(ValueError):
         spinor.nonlocal_potential_kb(g["psi"], nlc, g["nl"], g["elkb"][:1], 1.0)
+
+
+def test_spinor_pipeline_matches_reference(golden):
+    """The reference's whole spinor program on the fixture system (energy
+    range, coefficients, start states, filtering, portho, Hmat, sigma) against
+    the oracle's restatement."""
+    from oracle import oracle as O
+
+    g, nlc = load(golden)
+    dims = tuple(int(v) for v in g["dims"])
+    n = int(np.prod(dims))
+    h = float(g["h"])
+    dv = h ** 3
+    hargs = (g["potl"], g["ksqr"], dims, nlc, g["nl"], h, dv)
+    # energy range: init_psi draws four component grids from its fixed seed
+    starts = O.start_states(-874917403, 4, n, dv)
+    vmin, dE = so.energy_range(list(starts), dv, *hargs)
+    assert abs(vmin - float(g["run_vmin"])) <= 1e-9 * abs(float(g["run_vmin"]))
+    assert abs(dE - float(g["run_dE"])) <= 1e-9 * float(g["run_dE"])
+    # the Newton coefficients are the filter's (complex, both parts used)
+    nc = int(g["run_nc"])
+    dE_r, vmin_r = float(g["run_dE"]), float(g["run_vmin"])
+    ar, ai, zn = O.coefficients(g["run_el"], nc, dE_r, vmin_r, (nc / (2.5 * dE_r)) ** 2)
+    assert np.array_equal(ar + 1j * ai, g["run_an"]) and np.array_equal(zn, g["run_zn"])
+    # start spinors: consecutive init_psi draws, spin up then down
+    ns, ms = int(g["run_ns"]), int(g["run_ms"])
+    st = O.start_states(int(g["run_seed"]), 2 * ns, n, dv)
+    spinors = [np.concatenate([st[2 * j], st[2 * j + 1]]) for j in range(ns)]
+    ev, sig = so.pipeline(spinors, g["run_an"], g["run_zn"], 4.0 / dE_r, vmin_r, dv, *hargs)
+    assert len(ev) == int(g["run_mkept"])
+    assert np.allclose(ev, g["run_eval"], rtol=1e-9, atol=1e-12)
+    assert np.allclose(sig, g["run_sigma"], rtol=1e-7, atol=1e-10)
