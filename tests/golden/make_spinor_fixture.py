@@ -125,6 +125,7 @@ def main():
     an = rng.normal(size=ms * nc) + 1j * rng.normal(size=ms * nc)
     zn = rng.uniform(-2.0, 2.0, size=nc)
     par.dE_1, par.Vmin = 4.0 / 3.5, -0.45
+    filt_dE_1, filt_vmin = par.dE_1, par.Vmin        # the pipeline run below resets par
     ist.flagkb, ist.ms, ist.nc = 0, ms, nc
     psin = psi.copy()
     psim1 = np.zeros_like(psi)
@@ -223,7 +224,7 @@ def main():
                         vx=vx, vy=vy, vz=vz, rxyz=rxyz, vso=vso, rnlcut2=rnlcut2, nnlc=width,
                         nlc=keep.view(np.uint8).reshape(nat, width, NLC_DTYPE.itemsize), nl=nl,
                         elkb=elkb, psi=psi, ksqr=ksqr, potl=potl, an=an.reshape(ms, nc), zn=zn,
-                        dE_1=par.dE_1, vmin=par.Vmin, **outputs)
+                        dE_1=filt_dE_1, vmin=filt_vmin, **outputs)
     print("nl", nl, "|gauss|", np.abs(out_g).max(), "|kb|", np.abs(out_k).max(),
           "|H psi|", np.abs(hpsi["gauss"]).max(), "|filter|", np.abs(psims).max())
 
