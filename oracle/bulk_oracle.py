@@ -1,9 +1,9 @@
 """CPU restatement of the reference's bulk band-structure path
 (pseudopotFitting/): TEST INFRASTRUCTURE ONLY.
 
-Only tests/, the package smoke check and bench.py's CPU-baseline leg use this
-module, as the checker; the product computes band structures on the GPU
-(csrc/sep_bulk.cu) and never imports it.
+Only tests/ and bench.py's CPU leg use this module, as the checker; the
+product computes band structures on the GPU (csrc/sep_bulk.cu) and never
+imports it.
 
 Pinned against the reference's published runs (pseudopotFitting/TESTS,
 tests/golden/bulk_fit.json): the zincblende CdSe band structure at its input
