@@ -74,6 +74,7 @@ def datasets():
     d["K_nopsi"] = {"eval.dat": eval_text([(0, -0.3, 1e-3)])}
     d["L_hex"] = {"eval.dat": b"0 0x1p-3 1e-3\n", "psi.dat": psi_bytes(rng, 1)}
     d["M_grid"] = {"input.par": b"3 4 0\n"}
+    d["N_link"] = {"->": b"B"}                       # a symbolic link to B
     return d
 
 
@@ -95,13 +96,20 @@ CASES = [
     ("ngrid_mismatch", ["A", "--ngrid", "61"]),
     ("copy_conf_missing", ["C", "A", "--ngrid", "60", "--copy-conf"]),
     ("grid_nonpositive", ["A", "--grid-source", "M_grid/input.par"]),
+    ("symlink_and_dotdot", ["N_link", "C/../A", "--ngrid", "60"]),
+    ("absolute_names", ["D", "--ngrid", "60", "--eval-name", "{ROOT}/D/eval-x.dat",
+                        "--psi-name", "{ROOT}/D/psi-x.dat", "--output-dir", "{ROOT}/abs_out"]),
     ("no_grid", ["A"]),
     ("ngrid_zero", ["A", "--ngrid", "0"]),
 ]
 
 
 def materialise(root, sets):
+    """Writes the datasets under root; {"->": target} makes a symbolic link."""
     for name, files in sets.items():
+        if "->" in files:
+            os.symlink(files["->"].decode(), os.path.join(root, name))
+            continue
         os.makedirs(os.path.join(root, name), exist_ok=True)
         for fn, data in files.items():
             with open(os.path.join(root, name, fn), "wb") as f:
@@ -112,6 +120,7 @@ def run_case(script, sets, args):
     with tempfile.TemporaryDirectory() as tmp:
         root = str(Path(tmp).resolve())
         materialise(root, sets)
+        args = [a.replace("{ROOT}", root) for a in args]
         r = subprocess.run([sys.executable, script] + args, cwd=root, capture_output=True,
                            text=True)
         outdir = None

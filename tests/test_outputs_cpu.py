@@ -60,6 +60,9 @@ def test_writer_reports_unwritable_path(tmp_path):
 
 def materialise(fx, root):
     for name, files in fx["datasets"].items():
+        if "->" in files:                       # a symbolic link to another dataset
+            os.symlink(base64.b64decode(files["->"]).decode(), root / name)
+            continue
         os.makedirs(root / name, exist_ok=True)
         for fn, data in files.items():
             (root / name / fn).write_bytes(base64.b64decode(data))
@@ -71,8 +74,8 @@ def last_line(text):
 
 CASES = ["merge3", "grid_source", "names", "names_missing", "conf_differs", "psi_size",
          "not_sequential", "two_columns", "non_numeric", "hex_float", "empty_eval", "missing_psi",
-         "missing_dir", "ngrid_mismatch", "copy_conf_missing", "grid_nonpositive", "no_grid",
-         "ngrid_zero"]
+         "missing_dir", "ngrid_mismatch", "copy_conf_missing", "grid_nonpositive",
+         "symlink_and_dotdot", "absolute_names", "no_grid", "ngrid_zero"]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -81,7 +84,7 @@ def test_merge_matches_reference_script(fx, tmp_path, monkeypatch, capsys, name)
     root = tmp_path.resolve()
     materialise(fx, root)
     monkeypatch.chdir(root)
-    args = case["args"]
+    args = [a.replace("{ROOT}", str(root)) for a in case["args"]]
     rc, raised = None, None
     try:
         rc = outputs.main(args)
