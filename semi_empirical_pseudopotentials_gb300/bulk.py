@@ -336,6 +336,132 @@ def write_band_structure(path, kpts, bands):
             f.write("\n")
 
 
+_SEPARATION = "\n\n" + "*" * 63 + "\n\n"        # write.c:175-179
+
+
+def write_kpoints(path, kpts):
+    """kpoints_<i>.dat: x y z |k| per k-point, "% .10f" each (write.c:155-160)."""
+    with open(path, "w") as f:
+        for k in np.asarray(kpts):
+            f.write("% .10f % .10f % .10f % .10f\n" % (k[0], k[1], k[2], float(np.sqrt(k @ k))))
+
+
+def _pseudo_params(fit, theta):
+    """write.c:109-125: per crystal, per atom, the symbol and 4 parameters."""
+    out = []
+    for ci, c in enumerate(fit.crystals):
+        if ci:
+            out.append("\n")
+        out.append("\nBand structure %d\n" % ci)
+        for s in c.symbols:
+            p = fit_atom_params(fit, theta, ci, s)
+            out.append("\n%s" % s + "".join(" % .8f" % v for v in p))
+    return "".join(out)
+
+
+def _iteration(fit, theta, mse, it, n_iterations):
+    """write.c:72-80."""
+    text = (_SEPARATION if it != 0 else "") + "Iteration %d\nMSE % .5f\n" % (it, mse)
+    text += _pseudo_params(fit, theta)
+    if it == n_iterations:
+        text += _SEPARATION
+    return text
+
+
+def _input_summary(fit, n_iterations, nbv):
+    """write.c:128-152."""
+    out = ["INPUT\n\n",
+           "The number of band structures fit to was: %d\n" % len(fit.crystals),
+           "The kinetic energy scaling was: % .4f\n" % fit.ke_scale,
+           "The total number of iterations was: %d\n" % n_iterations,
+           "The beta used was: % .1f\n\n" % fit.beta,
+           "The atoms were place at the following positions:\n\n"]
+    for c in fit.crystals:
+        for s, t in zip(c.symbols, c.tau):
+            out.append("%s %.5f %.5f %.5f\n" % (s, t[0], t[1], t[2]))
+    for ci, c in enumerate(fit.crystals):
+        out += ["\nBand structure %d\n" % ci,
+                "The number of atoms in the cell was: %d\n" % len(c.symbols),
+                "The number of bands calculated was: %d\n" % c.ne,
+                "The number of k-points that were used to fit the pseudopotentials to was: "
+                "%d\n" % len(c.kpts),
+                "The maximum kinetic energy was: % .3f\n" % c.max_ke,
+                "The number of basis functions used was: %d\n" % nbv[ci]]
+    out.append(_SEPARATION)
+    return "".join(out)
+
+
+def write_results(directory, fit, theta, bands, best_mse, n_iterations, nbv):
+    """The files of writeResults and calcRealSpacePotential (write.c:7-69,
+    pot.c:21-83): kpoints_<i>.dat, output.dat, best_<Sym>_<i>_Params.dat,
+    bandStruct_<i>.dat and pot_<Sym>_<i>.dat."""
+    import time
+
+    from .binding import form_factor_table
+
+    d = str(directory)
+    for ci, c in enumerate(fit.crystals):
+        write_kpoints(os.path.join(d, "kpoints_%d.dat" % ci), c.kpts)
+    with open(os.path.join(d, "output.dat"), "w") as f:
+        f.write(time.ctime() + "\n" + _SEPARATION)
+        f.write("The best mean squared error found was: % .5f\n" % best_mse)
+        f.write(_pseudo_params(fit, theta) + _SEPARATION)
+        f.write(_input_summary(fit, n_iterations, nbv))
+    for ci, c in enumerate(fit.crystals):
+        for s in c.symbols:
+            p = fit_atom_params(fit, theta, ci, s)
+            with open(os.path.join(d, "best_%s_%d_Params.dat" % (s, ci)), "w") as f:
+                f.write("".join("% .8f\n" % v for v in p))
+        write_band_structure(os.path.join(d, "bandStruct_%d.dat" % ci), c.kpts, bands[ci])
+        for s in c.symbols:
+            r, v = form_factor_table(fit_atom_params(fit, theta, ci, s), c.vol_per_atom)
+            with open(os.path.join(d, "pot_%s_%d.dat" % (s, ci)), "w") as f:
+                f.write("".join("%g %g\n" % (x, y) for x, y in zip(r, v)))
+
+
+def run_fit(directory, steps=None, lr=1e-3, fitter=None, log_every=10):
+    """Fit the form-factor parameters of the run in ``directory`` with Adam on
+    the GPU gradient, in place of the reference's Monte Carlo search
+    (fit.c:9-69): reads its inputs, writes iterations.dat every log_every
+    steps as it does, and at the end its result files (``write_results``)
+    for the best parameters found.  The step of each parameter is lr times
+    its initial magnitude (at least 0.01).  steps defaults to input.par's
+    nIterations.  Returns (best parameters, best objective)."""
+    import time
+
+    d = str(directory)
+    fit = read_fit_inputs(d)
+    steps = fit.n_iterations if steps is None else int(steps)
+    bf = fitter(fit) if fitter is not None else BulkFit(fit)
+    theta = np.array(fit.params, dtype=np.float64)
+    scale = lr * np.maximum(np.abs(theta), 0.01)
+    m, v = np.zeros_like(theta), np.zeros_like(theta)
+    b1, b2, eps = 0.9, 0.999, 1e-12
+    val, grad = bf.objective_and_grad(theta)
+    best, best_theta = val, theta.copy()
+    with open(os.path.join(d, "iterations.dat"), "w") as f:
+        f.write(time.ctime() + "\n" + _SEPARATION + _iteration(fit, theta, val, 0, steps))
+    for it in range(1, steps + 1):
+        m = b1 * m + (1 - b1) * grad
+        v = b2 * v + (1 - b2) * grad * grad
+        mh, vh = m / (1 - b1 ** it), v / (1 - b2 ** it)
+        theta = theta - scale * mh / (np.sqrt(vh) + eps)
+        val, grad = bf.objective_and_grad(theta)
+        if val < best:
+            best, best_theta = val, theta.copy()
+        if it % log_every == 0:
+            with open(os.path.join(d, "iterations.dat"), "a") as f:
+                f.write(_iteration(fit, theta, val, it, steps))
+    with open(os.path.join(d, "iterations.dat"), "a") as f:
+        f.write(time.ctime() + "\n")
+    bands = bf.band_structures(best_theta)
+    nbv = [bc.nbv for bc in bf.crystals]
+    write_results(d, fit, best_theta, bands, best, steps, nbv)
+    if fitter is None:
+        bf.close()
+    return best_theta, best
+
+
 def _autograd():
     import torch
 
@@ -363,5 +489,27 @@ def __getattr__(name):
     raise AttributeError(name)
 
 
+def main(argv=None):
+    """python -m semi_empirical_pseudopotentials_gb300.bulk RUN_DIR [--steps N] [--lr X]"""
+    import argparse
+
+    p = argparse.ArgumentParser(description="Fit form-factor parameters to bulk band "
+                                "structures on the GPU (the inputs and outputs of "
+                                "pseudopotFitting/).")
+    p.add_argument("directory")
+    p.add_argument("--steps", type=int, default=None,
+                   help="optimiser steps (default: input.par's nIterations)")
+    p.add_argument("--lr", type=float, default=1e-3,
+                   help="step per parameter, relative to its initial magnitude")
+    a = p.parse_args(argv)
+    theta, best = run_fit(a.directory, a.steps, a.lr)
+    print("The best mean squared error found was: % .5f" % best)
+    return 0
+
+
 __all__ = ["Crystal", "FitInputs", "read_fit_inputs", "fit_atom_params", "basis", "BulkCrystal",
-           "BulkFit", "band_weights", "write_band_structure", "BandStructureMSE", "SepError"]
+           "BulkFit", "band_weights", "write_band_structure", "write_kpoints", "write_results",
+           "run_fit", "BandStructureMSE", "SepError"]
+
+if __name__ == "__main__":
+    raise SystemExit(main())

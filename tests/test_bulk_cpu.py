@@ -91,3 +91,54 @@ def test_band_structure_file_format(fits, tmp_path):
     want = fb.runs()["zb_cdse"]["bandStucture_0.dat"].splitlines()
     # the band columns are byte-identical; |k| is recomputed
     assert [g.split(" ", 2)[2] for g in got] == [w.split(" ", 2)[2] for w in want]
+
+
+class StubFit:
+    """Stands in for BulkFit in the driver's host logic: a quadratic
+    objective, and the oracle's band structures."""
+
+    def __init__(self, fit):
+        self.fit = fit
+        self.target = np.asarray(fit.params) * 1.01
+        self.crystals = [type("C", (), {"nbv": len(bo.basis(c.cell, c.max_ke))})()
+                         for c in fit.crystals]
+
+    def objective_and_grad(self, theta):
+        d = theta - self.target
+        return float(np.sum(d * d)), 2.0 * d
+
+    def band_structures(self, theta):
+        f = self.fit
+        return [bo.bands(c.cell, c.tau, [bulk.fit_atom_params(f, theta, ci, s) for s in c.symbols],
+                         c.kpts, c.max_ke, c.ne, f.ke_scale) for ci, c in enumerate(f.crystals)]
+
+
+def test_fit_driver_writes_the_reference_files(tmp_path):
+    d = fb.materialise("zb_cdse", str(tmp_path / "run"))
+    pub = fb.runs()["zb_cdse"]
+    theta, best = bulk.run_fit(d, steps=0, fitter=StubFit)   # input.par: nIterations 0
+    out = lambda name: open(f"{d}/{name}").read()
+    # the inputs' k-points and real-space tables, byte for byte (write.c:155-160, pot.c:73-77)
+    assert out("kpoints_0.dat") == pub["kpoints_0.dat"]
+    assert out("pot_Cd_0.dat") == pub["pot_Cd_0.dat"]
+    assert out("pot_Se_0.dat") == pub["pot_Se_0.dat"]
+    # the parameter block of output.dat as the reference printed it
+    block = pub["output.dat"].split("The best mean squared error found was:")[1]
+    block = block.split("\n", 1)[1].split("*****")[0].rstrip()
+    assert block in out("output.dat")
+    assert "The number of basis functions used was: 199\n" in out("output.dat")
+    assert out("best_Cd_0_Params.dat") == " 0.04248460\n 0.67188400\n 0.13608200\n 0.51454400\n"
+    got = np.loadtxt(f"{d}/bandStruct_0.dat")[:, 1:]
+    assert np.abs(got - fb.published_bands("zb_cdse", 0)[1]).max() < 2e-5
+
+
+def test_fit_driver_iterations_log(tmp_path):
+    d = fb.materialise("zb_cdse", str(tmp_path / "run"))
+    theta, best = bulk.run_fit(d, steps=20, lr=0.002, fitter=StubFit)
+    log = open(f"{d}/iterations.dat").read()
+    assert [l for l in log.splitlines() if l.startswith("Iteration")] == \
+        ["Iteration 0", "Iteration 10", "Iteration 20"]
+    mses = [float(l.split()[1]) for l in log.splitlines() if l.startswith("MSE")]
+    assert mses[-1] < mses[0]
+    fit = bulk.read_fit_inputs(d)
+    assert best < float(np.sum((fit.params - fit.params * 1.01) ** 2))

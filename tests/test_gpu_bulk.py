@@ -137,3 +137,16 @@ def test_bad_arguments_are_reported():
                      kpts=np.zeros((1, 3)), max_ke=1.0, ne=10 ** 6, scale=10.0)
     with pytest.raises(bulk.SepError):
         bulk.BulkCrystal(c)
+
+
+def test_fit_driver_on_the_gpu(tmp_path):
+    d = fb.materialise("zb_cdse", str(tmp_path / "run"))
+    fit = bulk.read_fit_inputs(d)
+    bf = bulk.BulkFit(fit)
+    start = bf.objective(fit.params)
+    bf.close()
+    theta, best = bulk.run_fit(d, steps=3, lr=1e-3)
+    assert best <= start * (1 + 1e-9)
+    for name in ("iterations.dat", "output.dat", "bandStruct_0.dat", "kpoints_0.dat",
+                 "pot_Cd_0.dat", "best_Se_0_Params.dat"):
+        assert (tmp_path / "run" / name).exists(), name
