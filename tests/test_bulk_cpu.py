@@ -142,3 +142,39 @@ def test_fit_driver_iterations_log(tmp_path):
     assert mses[-1] < mses[0]
     fit = bulk.read_fit_inputs(d)
     assert best < float(np.sum((fit.params - fit.params * 1.01) ** 2))
+
+
+# full-precision pins against the reference's own compiled code
+# (tests/golden/bulk_ref.npz, from tests/golden/make_bulk_fixture.py)
+@pytest.mark.parametrize("run", ["zb_cdse", "w_cdse", "cdse"])
+def test_oracle_bands_and_objectives_match_reference_code(fits, golden, run):
+    ref = golden("bulk_ref.npz")
+    fit = fits[run]
+    best = fb.best_atom_params(run)
+    bands = [bo.bands(c.cell, c.tau, best[i], c.kpts, c.max_ke, c.ne, fit.ke_scale)
+             for i, c in enumerate(fit.crystals)]
+    assert np.abs(np.concatenate([b.ravel() for b in bands]) - ref[f"{run}_bands"]).max() < 1e-10
+    # the fit objective of BulkFit (host arithmetic) on the reference's bands
+    stub = type("S", (), {"fit": fit})()
+    off, terms_w, terms = 0, [], []
+    for i, c in enumerate(fit.crystals):
+        n = c.ne * len(c.kpts)
+        b = ref[f"{run}_bands"][off:off + n].reshape(len(c.kpts), c.ne)
+        off += n
+        terms_w.append(bulk.BulkFit._mse_terms(stub, i, b, True)[0])
+        terms.append(bulk.BulkFit._mse_terms(stub, i, b, False)[0])
+    assert abs(np.mean(terms_w) - float(ref[f"{run}_weighted_mse"])) <= 1e-13 * np.mean(terms_w)
+    assert abs(np.mean(terms) - float(ref[f"{run}_mse"])) <= 1e-13 * np.mean(terms)
+
+
+@pytest.mark.parametrize("run", ["zb_cdse", "cdse"])
+def test_basis_matches_reference_code(fits, golden, run):
+    ref = golden("bulk_ref.npz")
+    for i, c in enumerate(fits[run].crystals):
+        g = bulk.basis(c.cell, c.max_ke)
+        r = ref[f"{run}_basis_{i}"]
+        assert len(g) == int(ref[f"{run}_nbv_{i}"]) == len(r)
+        key = lambda a: sorted(map(tuple, np.round(a, 10)))
+        assert key(g) == key(r)
+        # the same shells in the same order of |G|
+        assert np.allclose(np.sqrt((g * g).sum(1)), np.sqrt((r * r).sum(1)), rtol=0, atol=1e-12)

@@ -18,7 +18,7 @@ def fits(tmp_path_factory):
 
 
 @pytest.mark.parametrize("run,i", [("zb_cdse", 0), ("w_cdse", 0), ("cdse", 1)])
-def test_bands_match_oracle_and_published(fits, run, i):
+def test_bands_match_oracle_and_published(fits, golden, run, i):
     c = fits[run].crystals[i]
     bc = bulk.BulkCrystal(c, fits[run].ke_scale)
     p = bc.type_params(fb.best_atom_params(run)[i])
@@ -27,6 +27,11 @@ def test_bands_match_oracle_and_published(fits, run, i):
                    fits[run].ke_scale)
     assert np.abs(got - ref).max() < 1e-8                # eV
     assert np.abs(got - fb.published_bands(run, i)[1]).max() < 1.2e-5
+    # the reference's own calcBandStructure in full precision
+    full = golden("bulk_ref.npz")[f"{run}_bands"]
+    off = sum(cc.ne * len(cc.kpts) for cc in fits[run].crystals[:i])
+    mine = full[off:off + c.ne * len(c.kpts)].reshape(len(c.kpts), c.ne)
+    assert np.abs(got - mine).max() < 1e-8
     bc.close()
 
 
