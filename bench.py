@@ -435,16 +435,39 @@ def cpu_baseline(S, pot, dE, an_re, zn, vmin, seconds=12.0):
 
 
 # ---------------------------------------------------------------------------
+def _systems_module():
+    """The synthetic-input module (pure numpy), loaded from its file so that
+    the reference arm never imports the product package or its library."""
+    import importlib.util
+
+    path = os.path.join(ROOT, "semi_empirical_pseudopotentials_gb300", "systems.py")
+    spec = importlib.util.spec_from_file_location("sep_bench_systems", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def run_reference(args):
-    """--impl reference: the reference's CPU filter (oracle port) on host cores."""
+    """--impl reference: the reference's CPU filter on the host cores.  The
+    reference is a C program without a Python package; on the GPU machine (Arm, no
+    checkout) its filter is the oracle's C restatement, pinned bit for bit /
+    to 1e-11 against the reference's own sources.  Tables, V(r), k^2, start
+    states and Newton coefficients all come from the oracle: nothing of the
+    product package or libsep_gb300.so is loaded by this arm."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import semi_empirical_pseudopotentials_gb300 as sep  # host helpers only
     from oracle import oracle as O
 
-    S = build_system()
-    tr, tv = tables(sep, S)
+    w = WORKLOAD
+    S = _systems_module().make_system(w["name"], w["radius_nm"], w["n"], w["ms"], w["ns"],
+                                      w["nc"], seed=w["seed"], elmin=w["elmin"],
+                                      elmax=w["elmax"])
+    tr = np.zeros((2, 1024))
+    tv = np.zeros((2, 1024))
+    for t in (0, 1):
+        r, v = O.form_factor_table(S.params[t], S.vol_per_atom)
+        tr[t], tv[t] = r, O.shift_table(v)
     pot = O.vbuild(*S.xyz.T, S.types, tr, tv, [1024, 1024], S.dims, S.mins, S.steps)
     vmin = float(pot.min())
     ks = O.ksqr(*S.dims, *S.steps)
@@ -452,7 +475,7 @@ def run_reference(args):
     dE = 80.0  # fixed spectral width for the timing sample (the coefficients' values do not
     #            change the cost of a Newton step)
     nc = 1024
-    an_re, _, zn = sep.coefficients(S.el, nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
+    an_re, _, zn = O.coefficients(S.el, nc, dE, vmin, (nc / (2.5 * dE)) ** 2)
     cores = os.cpu_count() or 1
     ns = cores
     start = O.start_states(START_SEED, ns, S.ngrid, S.dv)

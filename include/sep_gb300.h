@@ -290,9 +290,12 @@ int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
  *  - Limit: m <= 1024 states per call (SEP_ERR_ARG above that; split the
  *    block).  ngrid is not limited.
  *  - Device: the calling thread's current device; psi_dev must live there.
- *    The first call on each device looks up the scratch address there
- *    (cudaGetSymbolAddress); make that first call before any stream capture
- *    begins.
+ *    Each call made outside stream capture looks up the scratch address in
+ *    the current context (cudaGetSymbolAddress), so it stays valid after
+ *    cudaDeviceReset and in non-primary contexts; a call made while
+ *    cuda_stream captures reuses the last address found on that device, so
+ *    make the first call on each device before any stream capture begins
+ *    (a first call during capture returns SEP_ERR_ARG).
  *  - Asynchronous on cuda_stream (a cudaStream_t; NULL = the legacy default
  *    stream): the states are normalised when the stream reaches the call.
  *  - Calls that overlap on one device (other streams or threads, not

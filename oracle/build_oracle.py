@@ -13,7 +13,17 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DEFAULT = "/root/reference"
+
+
+def reference_dir(ref=None):
+    """The reference checkout: `ref` when given, else $SEP_REFERENCE, else a
+    directory named ``reference`` beside this repository's root."""
+    if ref:
+        return ref
+    env = os.environ.get("SEP_REFERENCE")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def openblas_path():
@@ -45,7 +55,7 @@ def build_oracle(verbose=False):
 
 def build_ref(ref=None, verbose=False):
     """Compile the reference's sources into _ref/ when the checkout exists."""
-    ref = ref or os.environ.get("SEP_REFERENCE", REF_DEFAULT)
+    ref = reference_dir(ref)
     if not os.path.isdir(os.path.join(ref, "filter")):
         return None
     blas = openblas_path()

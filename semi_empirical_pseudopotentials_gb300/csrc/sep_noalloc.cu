@@ -39,15 +39,28 @@ constexpr int kNoallocMaxDevices = 64;
 std::mutex noalloc_mu;
 double* noalloc_ptr[kNoallocMaxDevices] = {};
 
-// Device address of noalloc_scratch on the current device, looked up once
-// per device (the first call on a device does this set-up).
-int noalloc_scratch_ptr(int dev, double** out) {
+// Device address of noalloc_scratch in the current context of device `dev`.
+// Outside stream capture it is looked up on every call, so the address stays
+// right after cudaDeviceReset (which recreates the module) and in a context
+// other than the primary one.  While `s` captures, the address of the last
+// lookup on that device is used: the first call on a device, which does the
+// lookup, has to come before any capture begins.
+int noalloc_scratch_ptr(int dev, cudaStream_t s, double** out) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;  // treat an unknown state as capturing
+  }
   std::lock_guard<std::mutex> lock(noalloc_mu);
-  if (!noalloc_ptr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, noalloc_scratch);
+    e = cudaGetSymbolAddress(&p, noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc_scratch)", __LINE__);
     noalloc_ptr[dev] = static_cast<double*>(p);
+  } else if (!noalloc_ptr[dev]) {
+    return arg_fail("sep_normalize_states_noalloc: first call on this device made during "
+                    "stream capture; make one call before capturing");
   }
   *out = noalloc_ptr[dev];
   return kOk;
@@ -73,10 +86,10 @@ int sep_normalize_states_noalloc(double* psi_dev, long m, long ngrid, double dv,
   }
   if (dev < 0 || dev >= kNoallocMaxDevices)
     return arg_fail("sep_normalize_states_noalloc: device ordinal above 63");
-  double* scratch = nullptr;
-  int r = noalloc_scratch_ptr(dev, &scratch);
-  if (r != kOk) return r;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  double* scratch = nullptr;
+  int r = noalloc_scratch_ptr(dev, s, &scratch);
+  if (r != kOk) return r;
   e = normalize_rows<double>(psi_dev, m, ngrid, dv, scratch, scratch + reduce_partial_doubles(m), s);
   if (e != cudaSuccess) return cuda_fail(e, "sep_normalize_states_noalloc", __LINE__);
   return kOk;

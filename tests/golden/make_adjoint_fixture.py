@@ -32,7 +32,7 @@ from oracle import build_oracle  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from semi_empirical_pseudopotentials_gb300 import systems  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = build_oracle.reference_dir(sys.argv[1] if len(sys.argv) > 1 else None)
 RADIUS_NM, N, NS, NC, SEED = 0.6, 32, 16, 8192, -314159
 WINDOWS = {"vb": (-0.233, -0.229), "cb": (-0.091, -0.050)}
 N_VB, N_CB = 3, 4

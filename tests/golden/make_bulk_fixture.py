@@ -2,7 +2,7 @@
 
 Run in a container that has the reference checkout (not on a GPU machine):
 
-    python tests/golden/make_bulk_fixture.py /root/reference
+    python tests/golden/make_bulk_fixture.py [REFERENCE_CHECKOUT]
 
 It copies the text of the reference's published fitting runs
 (pseudopotFitting/TESTS/{zb_cdse,w_cdse,cdse}: the inputs, output.dat, the
@@ -30,7 +30,10 @@ KEEP = ("pot_Cd_0.dat", "pot_Se_0.dat")      # zb_cdse only: the real-space tabl
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", ".."))
+    from oracle.build_oracle import reference_dir
+
+    ref = reference_dir(sys.argv[1] if len(sys.argv) > 1 else None)
     out = {}
     for run in RUNS:
         d = os.path.join(ref, "pseudopotFitting", "TESTS", run)

@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 from oracle import build_oracle  # noqa: E402
 from semi_empirical_pseudopotentials_gb300 import systems  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = build_oracle.reference_dir(sys.argv[1] if len(sys.argv) > 1 else None)
 
 
 # ---- filter/fd.h:23-36 struct layouts --------------------------------------

@@ -2,7 +2,7 @@
 
 Run in a container that has the reference checkout (not on a GPU machine):
 
-    python tests/golden/make_output_fixtures.py /root/reference
+    python tests/golden/make_output_fixtures.py [REFERENCE_CHECKOUT]
 
 It writes tests/golden/output_formats.json with
 * the text of In13_P16's eval.dat (filterStrainCube/main.c:163-166,
@@ -135,12 +135,18 @@ def run_case(script, sets, args):
                 if fn == "merge_manifest.txt":
                     data = data.replace(root.encode(), b"{ROOT}")
                 files[fn] = b64(data)
+        # the script's own location (in tracebacks) is replaced by {SCRIPT_DIR}
+        sdir = os.path.dirname(os.path.abspath(script))
         return {"rc": r.returncode, "stdout": r.stdout.replace(root, "{ROOT}"),
-                "stderr": r.stderr.replace(root, "{ROOT}"), "files": files}
+                "stderr": r.stderr.replace(root, "{ROOT}").replace(sdir, "{SCRIPT_DIR}"),
+                "files": files}
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", ".."))
+    from oracle.build_oracle import reference_dir
+
+    ref = reference_dir(sys.argv[1] if len(sys.argv) > 1 else None)
     script = os.path.join(ref, "combine_filter_outputs.py")
     in13 = os.path.join(ref, "filterStrainCube", "test", "In13_P16")
     sets = datasets()

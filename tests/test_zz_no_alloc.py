@@ -57,6 +57,33 @@ def test_noalloc_normalize_matches_allocating_entry_point_twice():
         assert np.allclose(np.sum(got * got, axis=1) * dv, 1.0, rtol=1e-12, atol=0.0)
 
 
+def test_noalloc_back_to_back_calls_without_synchronising():
+    """Several calls of different sizes queued on one stream, then on the NULL
+    (legacy default) stream, with one synchronise at the end of each run: the
+    shared scratch is reused by each call after the previous one finished on
+    the stream, and every block matches the allocating entry point."""
+    torch = pytest.importorskip("torch")
+    L = _lib()
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(77)
+    shapes = [(1024, 2048), (3, 50000), (1, 17), (513, 4096), (64, 36 * 36 * 36)]
+    blocks = [rng.standard_normal(s) * rng.uniform(0.5, 4.0, (s[0], 1)) for s in shapes]
+    dv = 0.42
+    refs = [_reference(L, b, dv) for b in blocks]
+    for stream in (torch.cuda.Stream(0), None):
+        devs = [torch.from_numpy(b).to("cuda:0") for b in blocks]
+        torch.cuda.synchronize()
+        handle = None if stream is None else C.c_void_p(stream.cuda_stream)
+        for d in devs:
+            m, n = d.shape
+            st = L.sep_normalize_states_noalloc(C.c_void_p(d.data_ptr()), m, n, dv, handle)
+            assert st == 0, L.sep_last_error()
+        torch.cuda.synchronize()
+        for d, ref in zip(devs, refs):
+            got = d.cpu().numpy()
+            assert np.allclose(got, ref, rtol=RTOL, atol=0.0), np.abs(got - ref).max()
+
+
 def test_noalloc_rejects_more_states_than_its_scratch_holds():
     torch = pytest.importorskip("torch")
     L = _lib()
