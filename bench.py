@@ -42,6 +42,26 @@ WORKLOAD = dict(name="r2.5nm_128", radius_nm=2.5, n=128, ms=8, ns=64, nc=1024, s
 # (0.126 against 0.144 ms per step at 32 pairs) for 17 GB more history
 BLOCK_STEPS = 64
 START_SEED = -271828
+# Time to band-edge eigenpairs, on a case where both precisions converge: the
+# same 2.5 nm sphere and 128^3 grid with the fitted CdSe form factors of the
+# reference's pseudopotFitting/TESTS/zb_cdse (dE = 16.5 Ha).  The gap lies
+# between the valence top (-0.230 Ha) and the 1S_e state (-0.147 Ha); one
+# conduction-edge window of 6 targets over [-0.165, -0.125] Ha, 16 start
+# states, nc = 4096.  The band-edge eigenpairs are the 4 lowest conduction
+# states (1S_e and the 1P_e triplet).  The complex64 path adds the FP64
+# polish of the window's Ritz pairs (a wide Gaussian, 256 Newton steps).  The
+# valence top of this dot (states ~1e-4 Ha apart) stays unconverged in both
+# precisions at this filter length and is not part of the metric.
+EDGE = dict(ns=16, ms=6, nc=4096, elmin=-0.165, elmax=-0.125, n_edge=4, polish_nc=256,
+            polish_guard=0.01, sigma_max=1e-5, e_tol=1e-6)
+
+
+def bench_config(world):
+    """The `config` of both arms' JSON lines (the same workload)."""
+    return {"workload": "r2.5nm CdSe-like sphere (2317 atoms), 128^3, 64 start states x "
+                        "8 targets, nc 1024",
+            "l2": "inputs larger than L2 (about 45 GB of filter state)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
 
 
 def parse():
@@ -137,11 +157,81 @@ def warm_pipeline(sep):
     pot = (-2.0 * np.exp(-r2 / 20.0)).ravel()
     c = sep.Context((n, n, n), (0.8, 0.8, 0.8), potl=pot, precision="mixed")
     start = sep.start_states(-5, 4, n ** 3, 0.8 ** 3)
+    c.set_polish(16, 0.5)  # loads the FP64 filter path of a complex64 context too
     c.pipeline(start, [-1.5, -1.0], 64, float(pot.min()))
     c.ortho(np.random.default_rng(0).standard_normal((512, n ** 3)))
     c.close()
     # the Leja points of nc = 1024 (computed once per process and nc)
     sep.coefficients([-1.0], WORKLOAD["nc"], 1.0, -1.0, 1.0)
+
+
+def band_edge_case(sep):
+    """Time from start states to the band-edge eigenpairs (EDGE) through
+    sep_pipeline: energy range, filter, ortho, Rayleigh-Ritz, sigma (and, for
+    complex64, the FP64 polish).  A pair of the complex64 path counts when its
+    Ritz value is within e_tol of the FP64 path's and its sigma <= sigma_max;
+    the FP64 pairs are the n_edge lowest in the window with sigma <= sigma_max."""
+    from semi_empirical_pseudopotentials_gb300 import adjoint, systems
+
+    w = WORKLOAD
+    S = systems.make_system("r2.5nm_128_fitted", w["radius_nm"], w["n"], EDGE["ms"],
+                            EDGE["ns"], EDGE["nc"], params=systems.FITTED_CDSE)
+    types = S.types.astype(np.int32)
+    theta = np.stack([S.params[0], S.params[1]])
+    el = adjoint.window_targets(EDGE["elmin"], EDGE["elmax"], EDGE["ms"])
+    start = sep.start_states(START_SEED, EDGE["ns"], S.ngrid, S.dv)
+    for nc in (EDGE["nc"], EDGE["polish_nc"]):  # the Leja points, once per process and nc
+        sep.coefficients([-1.0], nc, 1.0, -1.0, 1.0)
+    out = {"workload": f"r2.5nm CdSe sphere ({S.natom} atoms), 128^3, fitted zb_cdse form "
+                       f"factors, {EDGE['ns']} start states x {EDGE['ms']} targets over "
+                       f"[{EDGE['elmin']}, {EDGE['elmax']}] Ha, nc {EDGE['nc']}",
+           "band_edge": f"the {EDGE['n_edge']} lowest conduction states (1S_e, 1P_e)",
+           "criteria": {"abs_E_vs_f64_Ha": EDGE["e_tol"], "sigma_max": EDGE["sigma_max"]}}
+    runs = {}
+    for tag, prec, pol in (("f64", "f64", 0), ("mixed", "mixed", EDGE["polish_nc"]),
+                           ("mixed_no_polish", "mixed", 0)):
+        ctx = sep.Context(S.dims, S.steps, precision=prec)
+        ctx.potential_from_params(S.xyz, types, theta, S.vol_per_atom, S.mins)
+        ctx.set_polish(pol, EDGE["polish_guard"])
+        vmin = ctx.info()["vmin"]
+        t0 = time.perf_counter()
+        res = ctx.pipeline(start, el, EDGE["nc"], vmin)
+        wall = time.perf_counter() - t0
+        ctx.close()
+        t = res["timing"]
+        runs[tag] = (res["eval"], res["sigma"])
+        out[tag] = {"seconds": t["total_s"], "wall_s": wall, "mkept": res["mkept"],
+                    "stages_s": {k: round(t[k], 3) for k in
+                                 ("energy_range_s", "filter_s", "ortho_s", "rayleigh_ritz_s",
+                                  "sigma_s", "polish_s")},
+                    "h_applies": t["h_applies"], "dE": t["dE"]}
+    # the n_edge lowest Ritz values at or above the window's lower end, paired
+    # in ascending order (degenerate partners pair one to one)
+    ev, sg = runs["f64"]
+    o = np.argsort(ev)
+    ok = o[ev[o] >= EDGE["elmin"]][:EDGE["n_edge"]]
+    ok = ok[sg[ok] <= EDGE["sigma_max"]]
+    table = []
+    for tag in ("mixed", "mixed_no_polish"):
+        em, sm = runs[tag]
+        om = np.argsort(em)
+        mine = om[em[om] >= EDGE["elmin"]][:EDGE["n_edge"]]
+        rows, good = [], 0
+        for i, j in zip(ok, mine):
+            d = abs(float(em[j] - ev[i]))
+            hit = d <= EDGE["e_tol"] and sm[j] <= EDGE["sigma_max"]
+            good += int(hit)
+            rows.append({"E_f64": float(ev[i]), "sigma_f64": float(sg[i]), "E": float(em[j]),
+                         "sigma": float(sm[j]), "abs_dE_Ha": d, "converged": bool(hit)})
+        out[tag]["band_edge_pairs"] = rows
+        out[tag]["converged"] = good
+        if tag == "mixed":
+            table = rows
+    out["f64"]["converged"] = int(len(ok))
+    out["all_converged"] = bool(len(ok) == EDGE["n_edge"] and
+                                all(r["converged"] for r in table))
+    out["speedup_mixed_over_f64"] = out["f64"]["seconds"] / out["mixed"]["seconds"]
+    return out
 
 
 def subspace_gram(sep, ctx, psi_d, m, n, dv, peaks):
@@ -495,8 +585,9 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * T / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "r2.5nm CdSe-like sphere, 128^3, 64 states x 8 targets, "
-                                   "nc 1024", "step": f"{ns} states x {ncs - 1} Newton steps"},
+            "config": bench_config(args.gpus),
+            "workload_detail": {"precision": "FP64 (the reference's)",
+                                "step": f"{ns} states x {ncs - 1} Newton steps"},
             "cpu_baseline": {"value": value, "unit": "applies/s", "cores": cores, "kind": "port",
                              "sample": f"{ns} start states x {ncs - 1} Newton steps per step"},
             "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0,
@@ -671,8 +762,15 @@ def run_sep(args):
                 "max": float(d.max()), "median": float(np.median(d)),
                 "per_eigenvalue": [[float(e), float(x)] for e, x in zip(e64[:24], d[:24])]}
         ttb["speedup_mixed_over_f64"] = ttb["f64"]["seconds"] / ttb["mixed"]["seconds"]
-        extras["time_to_band_edge"] = ttb
+        ttb["note_convergence"] = (
+            "seeded a0 = +-10 form factors (the headline workload): dE ~ 80 Ha, each "
+            "Gaussian ~0.19 Ha wide against level spacings ~1e-3 Ha, so the window's Ritz "
+            "pairs stay unconverged in both precisions; time_to_band_edge holds the "
+            "converging case")
         ctx64.close()
+        del ctx64
+        extras["time_to_band_edge"] = band_edge_case(sep)
+        extras["time_to_band_edge_seeded_a0_10_unconverged"] = ttb
         extras["in13_p16_fixture"] = in13_case()
         extras["bulk_fit_cdse"] = bulk_case()
         try:
@@ -680,6 +778,8 @@ def run_sep(args):
         except Exception as exc:  # the operator's numbers are an extra, not the bench line
             extras["spinor_vso"] = {"error": f"{type(exc).__name__}: {exc}"}
         extras["cpu_baseline"] = cpu_baseline(S, pot, dE, an_re, zn, vmin)
+        # like-for-like precision: the FP64 GPU filter against the FP64 CPU port
+        extras["fp64"]["vs_cpu_port"] = extras["fp64"]["value"] / extras["cpu_baseline"]["value"]
 
     if rank == 0:
         # pack, first forward transform, per Newton step 2 (fused xy plane pass,
@@ -691,13 +791,10 @@ def run_sep(args):
                 "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "c64",
                 "data": "synthetic",
-                "config": {"workload": "r2.5nm CdSe-like sphere (2317 atoms), 128^3, "
-                                       "64 start states x 8 targets, nc 1024",
-                           "precision": "complex64 filter, FP32 accumulation",
-                           "newton_steps_per_accumulation": BLOCK_STEPS,
-                           "l2": "inputs larger than L2 (about 45 GB of filter state)",
-                           "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                           "dE": dE, "power_iterations": iters},
+                "config": bench_config(world),
+                "workload_detail": {"precision": "complex64 filter, FP32 accumulation",
+                                    "newton_steps_per_accumulation": BLOCK_STEPS,
+                                    "dE": dE, "power_iterations": iters},
                 "e2e": e2e, "gpu_launches": launches_step * args.steps,
                 "clocks": clk.summary()}
         line.update(extras)

@@ -45,6 +45,7 @@ typedef struct {
   double energy_range_s, filter_s, ortho_s, rayleigh_ritz_s, sigma_s, total_s;
   long power_iterations, mkept, h_applies;
   double emax, dE, dt;
+  double polish_s;  /* the FP64 polish of sep_ctx_set_polish (0 when off) */
 } sep_timing;
 
 /* ---- library ------------------------------------------------------------ */
@@ -87,6 +88,20 @@ int sep_ctx_set_fusion(sep_ctx *ctx, int enable);
  * states on the device and is skipped when it does not fit.  The refinement
  * time is counted in rayleigh_ritz_s. */
 int sep_ctx_set_refine(sep_ctx *ctx, int steps);
+/* FP64 polish that sep_pipeline runs after sigma (default off, nc = 0): the
+ * Ritz pairs whose values lie in [el_min - guard, el_max + guard] are
+ * filtered once more in FP64 by one wide Gaussian at the window's centre
+ * (filter/filter.c:59-83 with nc Newton steps, dt = (nc / 2.5 dE)^2 as
+ * filter/main.c:70), then orthonormalised (filter/ortho.c:11-52),
+ * diagonalised (filter/Hmat.c:11-86) and their sigma recomputed
+ * (filter/energy.c:88-119); the block replaces its rows of psi, eval and
+ * sige.  Meant for complex64 filters: their Ritz vectors carry broadband
+ * single-precision rounding noise that holds sigma near 1e-4 Ha while their
+ * Ritz values already match the FP64 path; the wide Gaussian damps the noise
+ * far from the window.  No counterpart in the reference.  nc in {0} or
+ * [2, 8192]; guard >= 0 (hartree, default 0.01).  Its time is
+ * sep_timing.polish_s (also in total_s). */
+int sep_ctx_set_polish(sep_ctx *ctx, long nc, double guard);
 
 /* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------
  * hpsi = T psi + V psi for nstates complex grids (interleaved complex128). */
@@ -361,8 +376,12 @@ int sep_read_grid_source(const char *path, long *ngrid);
  * sep_bulk_bands_backward: given dL/dE (nk x nev, per eV), writes
  *   dL/dparams (ntype x 4) by Hellmann-Feynman (no reference counterpart:
  *   the reference fits by Monte Carlo, fit.c:9-69), and the bands when
- *   bands != NULL.  Degenerate bands must carry equal dL/dE for the result
- *   to be the gradient.
+ *   bands != NULL.  Where a k-point has degenerate bands (equal to 1e-10
+ *   relative) with unequal dL/dE, the sorted bands are not differentiable;
+ *   per parameter the result is then the limit of central differences,
+ *   from degenerate perturbation theory on each cluster (the eigenvalues of
+ *   U_c^H dV/dtheta U_c, up to 16 bands per cluster; bands past nev in a
+ *   cluster count with dL/dE = 0).
  * sep_bulk_solver_path: 1 when the batched eigensolver ran, 0 when the
  *   matrices went one per call, -1 before the first solve.
  * sep_bulk_set_solver: 1 (default) = the batched eigensolver, one matrix per

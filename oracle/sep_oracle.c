@@ -554,17 +554,24 @@ void orc_sigma(const orc_ctx *c, const double *psi, long m, double *sige) {
   free(hhz);
 }
 
+static int omp_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
 /* filter/main.c:92-98: the filter cycles of ns start states, one per OpenMP
  * thread as the reference runs them; returns the wall time in seconds. */
 double orc_filter_batch(const orc_ctx *c, long ns, const double *start, const double *an_re,
                         const double *zn, long ms, long nc, double dE_1, double vmin,
                         double *out, int nthreads) {
   const long n = c->ngrid;
-#ifdef _OPENMP
-  if (nthreads > 0) omp_set_num_threads(nthreads);
-#endif
+  /* the thread count applies to this region only (no process-wide setting) */
+  const int nt = nthreads > 0 ? nthreads : omp_max_threads();
   double t0 = now_s();
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
   for (long s = 0; s < ns; s++)
     orc_filter_cycle(c, start + (size_t)s * n, an_re, zn, ms, nc, dE_1, vmin,
                      out + (size_t)s * ms * n);
@@ -592,10 +599,8 @@ long orc_pipeline(const orc_ctx *c, long ns, long ms, long nc, const double *el,
   orc_coefficients(ms, nc, dE, vmin, dt, el, an_re, an_im, zn);
   const double dE_1 = 4.0 / dE;
   t0 = now_s();
-#ifdef _OPENMP
-  if (nthreads > 0) omp_set_num_threads(nthreads);
-#endif
-#pragma omp parallel for schedule(dynamic, 1)
+  const int nt = nthreads > 0 ? nthreads : omp_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
   for (long s = 0; s < ns; s++) {
     /* filtering, filter.c:11-55: filter, normalise, energies of the block */
     double *blk = psitot + (size_t)s * ms * n;

@@ -33,7 +33,8 @@ class Timing(C.Structure):
                 ("ortho_s", C.c_double), ("rayleigh_ritz_s", C.c_double),
                 ("sigma_s", C.c_double), ("total_s", C.c_double),
                 ("power_iterations", C.c_long), ("mkept", C.c_long), ("h_applies", C.c_long),
-                ("emax", C.c_double), ("dE", C.c_double), ("dt", C.c_double)]
+                ("emax", C.c_double), ("dE", C.c_double), ("dt", C.c_double),
+                ("polish_s", C.c_double)]
 
 
 def lib():
@@ -95,6 +96,7 @@ def lib():
         L.sep_ctx_set_subspace.argtypes = [vp, C.c_int]
         L.sep_ctx_set_fusion.argtypes = [vp, C.c_int]
         L.sep_ctx_set_refine.argtypes = [vp, C.c_int]
+        L.sep_ctx_set_polish.argtypes = [vp, C.c_long, C.c_double]
         L.sep_subspace_gemm.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, C.c_double,
                                         C.c_int, dp]
         L.sep_subspace_rotate.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, dp]
@@ -380,6 +382,11 @@ class Context:
     def set_refine(self, steps):
         """FP64 residual-subspace steps after Rayleigh-Ritz in pipeline() (0..8)."""
         _check(lib().sep_ctx_set_refine(self.h, int(steps)))
+
+    def set_polish(self, nc, guard=0.01):
+        """FP64 polish of the window's Ritz pairs in pipeline(): nc Newton steps of
+        one wide Gaussian at the window centre (0 = off), guard in hartree."""
+        _check(lib().sep_ctx_set_polish(self.h, int(nc), float(guard)))
 
     def set_fusion(self, enable):
         """Fused xy plane pass for complex64 Newton steps (nx = ny in 64/96/128)."""

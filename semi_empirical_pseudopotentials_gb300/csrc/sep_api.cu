@@ -490,7 +490,7 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
     return arg_fail("sep_pipeline: bad argument");
   sep_timing t;
   std::memset(&t, 0, sizeof t);
-  cudaEvent_t ev[6];
+  cudaEvent_t ev[7];
   for (auto& e : ev) CK(cudaEventCreate(&e));
   const long long n = c->n;
   const long m = ns * ms;
@@ -525,23 +525,36 @@ int sep_pipeline(sep_ctx* c, const double* start, long ns, const double* el, lon
   CK(cudaEventRecord(ev[4], c->stream));
   RET(sigma_device(c, d_psi, k, sige, hpsi));
   CK(cudaEventRecord(ev[5], c->stream));
+  long polish_applies = 0;
+  if (c->polish_nc > 0) {
+    double lo = el[0], hi = el[0];
+    for (long e = 1; e < ms; ++e) {
+      lo = std::min(lo, el[e]);
+      hi = std::max(hi, el[e]);
+    }
+    RET(polish_device(c, d_psi, &k, lo, hi, dE, vmin, eval, sige, &polish_applies));
+  }
+  CK(cudaEventRecord(ev[6], c->stream));
   if (psi_out)
     CK(cudaMemcpyAsync(psi_out, d_psi, sizeof(double) * (size_t)n * k, cudaMemcpyDeviceToHost,
                        c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  float ms_[5];
-  for (int i = 0; i < 5; ++i) CK(cudaEventElapsedTime(&ms_[i], ev[i], ev[i + 1]));
+  float ms_[6];
+  for (int i = 0; i < 6; ++i) CK(cudaEventElapsedTime(&ms_[i], ev[i], ev[i + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
   t.energy_range_s = ms_[0] * 1e-3;
   t.filter_s = ms_[1] * 1e-3;
   t.ortho_s = ms_[2] * 1e-3;
   t.rayleigh_ritz_s = ms_[3] * 1e-3;
   t.sigma_s = ms_[4] * 1e-3;
-  t.total_s = t.energy_range_s + t.filter_s + t.ortho_s + t.rayleigh_ritz_s + t.sigma_s;
+  t.polish_s = ms_[5] * 1e-3;
+  t.total_s = t.energy_range_s + t.filter_s + t.ortho_s + t.rayleigh_ritz_s + t.sigma_s +
+              t.polish_s;
   t.mkept = k;
   t.dE = dE;
   t.dt = dt;
-  t.h_applies = (long)(t.power_iterations + 1) + (long)ns * (nc - 1) + (hpsi ? 1 : 2) * k;
+  t.h_applies = (long)(t.power_iterations + 1) + (long)ns * (nc - 1) + (hpsi ? 1 : 2) * k +
+                polish_applies;
   *mkept = k;
   if (timing) *timing = t;
   return kOk;
@@ -618,6 +631,14 @@ int sep_time_passes(sep_ctx* c, long npairs, int reps, double* ms_out) {
 int sep_ctx_set_refine(sep_ctx* c, int steps) {
   if (!c || steps < 0 || steps > 8) return arg_fail("sep_ctx_set_refine: steps in [0, 8]");
   c->refine_steps = steps;
+  return kOk;
+}
+
+int sep_ctx_set_polish(sep_ctx* c, long nc, double guard) {
+  if (!c || !(nc == 0 || (nc >= 2 && nc <= 8192)) || !(guard >= 0.0) || !std::isfinite(guard))
+    return arg_fail("sep_ctx_set_polish: nc in {0} or [2, 8192] and a finite guard >= 0");
+  c->polish_nc = nc;
+  c->polish_guard = guard;
   return kOk;
 }
 

@@ -859,6 +859,72 @@ int refine_device(sep_ctx* c, double* d_psi, long k, long m_cap, double* eval_ho
   return kOk;
 }
 
+// FP64 polish of the Ritz pairs in a target window (no counterpart in the
+// reference).  After a complex64 filter the Ritz vectors carry single-
+// precision rounding noise spread over the whole spectrum, most of it at high
+// wavenumbers; it bounds their residuals near 1e-4 Ha although their Ritz
+// values already agree with the FP64 path's.  The Ritz vectors whose values
+// lie in [elmin - guard, elmax + guard] are filtered once more, in FP64, by a
+// wide Gaussian at the window's centre (the Newton filter of
+// filter/filter.c:59-83 with one target and c->polish_nc steps), which damps
+// the components far from the window and leaves those inside it nearly
+// unchanged; the block is then orthonormalised and diagonalised again
+// (filter/ortho.c, filter/Hmat.c) and its residuals computed (energy.c:88-119).
+// The polished block replaces its rows of psi, eval and sige; *k shrinks when
+// ortho drops a direction.  *applies counts the FP64 H applies.
+int polish_device(sep_ctx* c, double* d_psi, long* k, double elmin, double elmax, double dE,
+                  double vmin, double* eval, double* sige, long* applies) {
+  *applies = 0;
+  const long nc = c->polish_nc;
+  const long m = *k;
+  if (nc < 2 || m < 1) return kOk;
+  const double lo = elmin - c->polish_guard, hi = elmax + c->polish_guard;
+  long i0 = 0;
+  while (i0 < m && eval[i0] < lo) ++i0;
+  long i1 = i0;
+  while (i1 < m && eval[i1] <= hi) ++i1;
+  const long kb = i1 - i0;
+  if (kb < 1) return kOk;
+  const long long n = c->n;
+  const size_t row = sizeof(double) * (size_t)n;
+  RET(grow(c, c->w_refine, row * (size_t)kb));
+  double* F = c->w_refine.as<double>();
+  const double center = 0.5 * (elmin + elmax);
+  const double dt = ((double)nc / (2.5 * dE)) * ((double)nc / (2.5 * dE));  // main.c:70
+  std::vector<double> ar((size_t)nc), ai((size_t)nc), zn((size_t)nc);
+  host::coefficients(1, nc, dE, vmin, dt, &center, ar.data(), ai.data(), zn.data());
+  RET(filter_impl<double>(c, d_psi + (size_t)i0 * n, kb, ar.data(), zn.data(), 1, nc,
+                          4.0 / dE, vmin, F, nullptr));
+  RET(normalize_device(c, F, kb));
+  long kb2 = 0;
+  RET(ortho_device(c, F, kb, &kb2));
+  RET(normalize_device(c, F, kb2));
+  std::vector<double> ev((size_t)kb2), sg((size_t)kb2);
+  double* hp = nullptr;
+  RET(rayleigh_ritz_device(c, F, kb2, ev.data(), &hp));
+  RET(normalize_device(c, F, kb2, hp));
+  RET(sigma_device(c, F, kb2, sg.data(), hp));
+  CK(cudaMemcpyAsync(d_psi + (size_t)i0 * n, F, row * (size_t)kb2, cudaMemcpyDeviceToDevice,
+                     c->stream));
+  const long drop = kb - kb2;
+  if (drop > 0) {  // rows after the block move up, one row per copy (no overlap)
+    for (long r = i1; r < m; ++r)
+      CK(cudaMemcpyAsync(d_psi + (size_t)(r - drop) * n, d_psi + (size_t)r * n, row,
+                         cudaMemcpyDeviceToDevice, c->stream));
+    for (long r = i1; r < m; ++r) {
+      eval[r - drop] = eval[r];
+      sige[r - drop] = sige[r];
+    }
+  }
+  for (long r = 0; r < kb2; ++r) {
+    eval[i0 + r] = ev[(size_t)r];
+    sige[i0 + r] = sg[(size_t)r];
+  }
+  *k = m - drop;
+  *applies = kb * (nc - 1) + (hp ? 1 : 2) * kb2;
+  return kOk;
+}
+
 // filter/energy.c:88-119: sigma = sqrt(<H^2> - <H>^2) = |H psi - E psi| for a
 // normalised psi (dv metric) with E = <psi|H|psi>.
 int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,

@@ -74,6 +74,8 @@ struct sep_ctx {
   bool use_graphs = true;
   int block_steps = 32;
   int refine_steps = 0;  // FP64 residual-subspace steps after Rayleigh-Ritz in sep_pipeline
+  long polish_nc = 0;     // FP64 polish of the window's Ritz pairs in sep_pipeline (0 = off)
+  double polish_guard = 0.01;  // hartree beyond the target window included in the polish
   int subspace_tc = 1;  // subspace contractions on the tensor cores (1) or the FP64 pipe (0)
   int fuse_xy = 1;      // complex64 Newton steps with the fused xy plane pass when it applies
   bool xy_ready = false;
@@ -121,6 +123,13 @@ int rayleigh_ritz_device(sep_ctx* c, double* d_psi, long m, double* eval_host,
 // *hpsi: H psi of the rows when known (as rayleigh_ritz_device returns it).
 int refine_device(sep_ctx* c, double* d_psi, long k, long m_cap, double* eval_host,
                   double** hpsi, long* k_out);
+// FP64 polish of the Ritz pairs whose values lie within c->polish_guard of
+// [elmin, elmax]: a wide FP64 Gaussian filter at the window's centre
+// (c->polish_nc Newton steps), then ortho, Rayleigh-Ritz and sigma of that
+// block, which replaces its rows (eval, sige on the host).  *k: row count in
+// and out; *applies: FP64 H applies made.
+int polish_device(sep_ctx* c, double* d_psi, long* k, double elmin, double elmax, double dE,
+                  double vmin, double* eval, double* sige, long* applies);
 // d_hpsi: H psi of these states when already known (no H applies then)
 int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,
                  const double* d_hpsi = nullptr);

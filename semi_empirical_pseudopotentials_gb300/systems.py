@@ -45,6 +45,14 @@ def zincblende_sphere(radius_nm, a_angstrom=6.08):
     return types.astype(np.int64), xyz
 
 
+# The fitted zincblende CdSe form factors a0..a3 of the reference's
+# pseudopotFitting/TESTS/zb_cdse (CdParams.par, SeParams.par).  With them the
+# band edges of a nanocrystal converge at a few thousand Newton steps; the
+# seeded a0 = +-10 set spreads the spectrum over ~80 Ha, too wide for that.
+FITTED_CDSE = {CATION: np.array([0.0424846, 0.671884, 0.136082, 0.514544]),
+               ANION: np.array([-0.22725, 3.69721, -2.24471, 0.676691])}
+
+
 def form_factor_params(seed):
     """Seeded a0..a3 per species (see module docstring)."""
     rng = np.random.default_rng(seed)
@@ -109,7 +117,9 @@ def _half(r):
     return float(np.rint(0.5 * (np.max(r) - np.min(r)) + 5.0))
 
 
-def make_system(name, radius_nm, n, ms, ns, nc=1024, seed=0, el=None, elmin=None, elmax=None):
+def make_system(name, radius_nm, n, ms, ns, nc=1024, seed=0, el=None, elmin=None, elmax=None,
+                params=None):
+    """params: type -> a0..a3 (e.g. FITTED_CDSE); None draws them from `seed`."""
     types, xyz_raw = zincblende_sphere(radius_nm)
     xyz = _center(xyz_raw)
     half = tuple(_half(xyz[:, d]) for d in range(3))
@@ -119,7 +129,9 @@ def make_system(name, radius_nm, n, ms, ns, nc=1024, seed=0, el=None, elmin=None
         lo = -0.40 if elmin is None else elmin
         hi = -0.10 if elmax is None else elmax
         el = lo + np.arange(ms) * ((hi - lo) / (ms - 1)) if ms > 1 else np.array([lo])
-    return System(name=name, dims=dims, types=types, xyz=xyz, xyz_raw=xyz_raw, params=form_factor_params(seed),
+    params = form_factor_params(seed) if params is None else {t: np.asarray(v, dtype=np.float64)
+                                                             for t, v in params.items()}
+    return System(name=name, dims=dims, types=types, xyz=xyz, xyz_raw=xyz_raw, params=params,
                   vol_per_atom=a ** 3 / 8.0, half=half, ms=ms, ns=ns, nc=nc,
                   el=np.asarray(el, dtype=np.float64), seed=seed)
 

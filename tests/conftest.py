@@ -1,7 +1,11 @@
 import os
 import sys
 
-import pytest
+# numpy's OpenBLAS threads spin between calls and starve the oracle's OpenMP
+# filter threads (the oracle's dgesvd/dsyev calls are small); one thread each
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
+import pytest  # noqa: E402
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:

@@ -17,7 +17,12 @@ Fixtures:
   Vmin, coefficient(), hamiltonian(), hnorm(), filter(), energy_all(),
   get_energy_range(), and a full fixed-seed filter_ref run (eval.dat).
 
-usage: python tests/golden/make_golden.py [/path/to/reference]
+* config0_ref.npz -- the reference's own filter program on the benchmark's
+  smallest configuration (CONFIG0) with a fixed start seed: eval.dat and the
+  run's dE, Vmin, dt.
+
+usage: python tests/golden/make_golden.py [/path/to/reference] [--config0]
+  (--config0: only config0_ref.npz)
 """
 import ctypes as C
 import os
@@ -34,7 +39,8 @@ sys.path.insert(0, ROOT)
 from oracle import build_oracle  # noqa: E402
 from semi_empirical_pseudopotentials_gb300 import systems  # noqa: E402
 
-REF = build_oracle.reference_dir(sys.argv[1] if len(sys.argv) > 1 else None)
+_ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
+REF = build_oracle.reference_dir(_ARGS[0] if _ARGS else None)
 
 
 # ---- filter/fd.h:23-36 struct layouts --------------------------------------
@@ -246,6 +252,38 @@ def small_reference_outputs():
     np.savez_compressed(os.path.join(HERE, "ref_small.npz"), **out)
 
 
+# The benchmark's smallest configuration: the 1.2 nm sphere (275 atoms) with
+# the seeded a0 = +-10 form factors on its 64^3 grid, 8 start states x 4
+# targets, nc = 1024, FP64.  The targets cover [-3.25, -2.95] Ha, the window
+# of the 128^3 benchmark workload.
+CONFIG0 = dict(radius_nm=1.2, n=64, ms=4, ns=8, nc=1024, seed=0, elmin=-3.25, elmax=-2.95,
+               start_seed=-271828)
+
+
+def config0_reference_run(nthreads=8):
+    """config0_ref.npz: the reference's own filter program (filter_ref, built by
+    oracle/Makefile.ref from filter/*.c) on CONFIG0 with a fixed start seed:
+    eval.dat (Ritz values, sigma), the kept count and its dE, Vmin, dt."""
+    refdir = build_oracle.build_ref(REF)
+    c = CONFIG0
+    S = systems.make_system("config0", c["radius_nm"], c["n"], c["ms"], c["ns"], c["nc"],
+                            seed=c["seed"], elmin=c["elmin"], elmax=c["elmax"])
+    tabs = {t: _form_factor_table(a, S.vol_per_atom) for t, a in S.params.items()}
+    with tempfile.TemporaryDirectory() as tmp:
+        systems.write_reference_inputs(S, tmp, nthreads=nthreads, tables=tabs)
+        res = subprocess.run([os.path.join(refdir, "filter_ref"), str(c["start_seed"]),
+                              str(nthreads)], cwd=tmp, capture_output=True, text=True,
+                             check=True)
+        ev = np.loadtxt(os.path.join(tmp, "eval.dat"))
+    out = dict(CONFIG0)
+    out.update(eval=ev[:, 1], sigma=ev[:, 2], mkept=len(ev))
+    for ln in res.stdout.splitlines():
+        if ln.startswith("nc = "):
+            f = ln.split()
+            out.update(dt=float(f[5]), dE=float(f[8]), vmin=float(f[11]))
+    np.savez_compressed(os.path.join(HERE, "config0_ref.npz"), **out)
+
+
 def _form_factor_table(a, vol):
     from oracle import oracle as O
 
@@ -253,9 +291,11 @@ def _form_factor_table(a, vol):
 
 
 if __name__ == "__main__":
-    fixture_in13()
-    fixture_zb_cdse()
-    small_reference_outputs()
+    if "--config0" not in sys.argv:
+        fixture_in13()
+        fixture_zb_cdse()
+        small_reference_outputs()
+    config0_reference_run()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -148,3 +148,30 @@ def test_in13_fixture_end_to_end():
         assert np.abs(ev - e).min() < 1e-6
     mine = (ev > -0.25) & (ev < 0.0) & (sg < 1e-5)
     assert mine.sum() == win.sum()
+
+
+def test_config0_end_to_end(golden):
+    """The benchmark's smallest configuration (1.2 nm sphere, 64^3, 8 states x
+    4 targets, nc 1024) through the oracle's whole path against the reference
+    program's own run (config0_ref.npz): dE, the kept count and the Ritz
+    values (1e-6 Ha; measured ~1e-10)."""
+    from semi_empirical_pseudopotentials_gb300 import adjoint, systems
+
+    g = golden("config0_ref.npz")
+    S = systems.make_system("config0", float(g["radius_nm"]), int(g["n"]), int(g["ms"]),
+                            int(g["ns"]), int(g["nc"]), seed=int(g["seed"]))
+    tr = np.zeros((2, 1024))
+    tv = np.zeros((2, 1024))
+    for t in (0, 1):
+        r, v = O.form_factor_table(S.params[t], S.vol_per_atom)
+        tr[t], tv[t] = r, O.shift_table(v)
+    pot = O.vbuild(*S.xyz.T, S.types, tr, tv, [1024, 1024], S.dims, S.mins, S.steps)
+    assert float(pot.min()) == float(g["vmin"])
+    octx = O.Context(S.dims, pot, O.ksqr(*S.dims, *S.steps), S.dv)
+    el = adjoint.window_targets(float(g["elmin"]), float(g["elmax"]), int(g["ms"]))
+    start = O.start_states(int(g["start_seed"]), S.ns, S.ngrid, S.dv)
+    res = octx.pipeline(start, el, int(g["nc"]), float(pot.min()))
+    assert abs(res["timing"]["dE"] - float(g["dE"])) <= 1e-10 * float(g["dE"])
+    assert res["mkept"] == int(g["mkept"])
+    assert np.abs(res["eval"] - g["eval"]).max() <= 1e-6
+    assert np.allclose(res["sigma"], g["sigma"], rtol=2e-5, atol=1e-6)
