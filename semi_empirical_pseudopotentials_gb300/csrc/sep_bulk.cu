@@ -52,7 +52,13 @@ struct sep_bulk {
   cuDoubleComplex* wmat = nullptr;  // nbv x nbv
   double* w = nullptr;        // nk x nbv eigenvalues
   double* bands = nullptr;    // nk x nev
-  double* dlde = nullptr;     // nk x nev
+  double* dlde = nullptr;     // nk x nev_cap (dL/dE per band, clusters widened past nev)
+  long nev_cap = 0;
+  // degenerate clusters with unequal dL/dE (sep_bulk_bands_backward)
+  int* clu = nullptr;                 // per cluster: k, first band, size
+  cuDoubleComplex* cluy = nullptr;    // per cluster and parameter: dV/dtheta U_c (nbv x c)
+  cuDoubleComplex* clum = nullptr;    // per cluster and parameter: U_c^H dV/dtheta U_c (c x c)
+  long clu_cap = 0;
   double* partials = nullptr; // grad blocks x 4 ntype
   double* grad = nullptr;     // 4 ntype
   int* info = nullptr;        // nk
@@ -245,6 +251,141 @@ __global__ void k_bulk_grad(const double* __restrict__ g, const double* __restri
   }
 }
 
+constexpr int kMaxCluster = 16;  // bands in one degenerate cluster handled exactly
+
+// dV_jl/da_{t,m} = sum_{a of type t} (cos - i sin)(G_jl . tau_a) / natom * dv_t/da_m(|G_jl|)
+__device__ __forceinline__ void dv_dparam(const double* __restrict__ g,
+                                          const double* __restrict__ tau,
+                                          const int* __restrict__ types,
+                                          const double* __restrict__ prm, int natom, long j,
+                                          long l, int ty, int m, double* re, double* im) {
+  const double dx = g[3 * j] - g[3 * l], dy = g[3 * j + 1] - g[3 * l + 1],
+               dz = g[3 * j + 2] - g[3 * l + 2];
+  const double q = sqrt(dot_rn(dx, dy, dz, dx, dy, dz));
+  const double q2 = __dmul_rn(q, q);
+  const double* p = prm + 4 * ty;
+  const double e = exp(p[3] * q2);
+  const double den = p[2] * e + 1.0;
+  const double num = q2 - p[1];
+  const double f_den2 = p[0] * num * e / (den * den);
+  const double d = m == 0 ? num / den : m == 1 ? -p[0] / den : m == 2 ? -f_den2
+                                                                        : -f_den2 * p[2] * q2;
+  const double inv = 1.0 / (double)natom;
+  double sr = 0.0, si = 0.0;
+  for (int a = 0; a < natom; ++a) {
+    if (types[a] != ty) continue;
+    const double ph = dot_rn(dx, dy, dz, tau[3 * a], tau[3 * a + 1], tau[3 * a + 2]);
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    sr += inv * cs;
+    si -= inv * sn;
+  }
+  *re = d * sr;
+  *im = d * si;
+}
+
+// Y = dV/da_{t,m} U_c for cluster c (grid: clusters x parameters; rows j over threads)
+__global__ void k_bulk_cluster_y(const double* __restrict__ g, const double* __restrict__ tau,
+                                 const int* __restrict__ types, const double* __restrict__ prm,
+                                 int natom, int nparam, long nbv,
+                                 const cuDoubleComplex* __restrict__ h,
+                                 const int* __restrict__ clu, cuDoubleComplex* __restrict__ y) {
+  const int item = blockIdx.x / nparam, par = blockIdx.x % nparam;
+  const int k = clu[3 * item], n0 = clu[3 * item + 1], c = clu[3 * item + 2];
+  const cuDoubleComplex* u = h + (long)k * nbv * nbv;
+  cuDoubleComplex* out = y + ((long)item * nparam + par) * nbv * kMaxCluster;
+  for (long j = threadIdx.x; j < nbv; j += blockDim.x) {
+    double ar[kMaxCluster], ai[kMaxCluster];
+#pragma unroll
+    for (int i = 0; i < kMaxCluster; ++i) ar[i] = ai[i] = 0.0;
+    for (long l = 0; l < nbv; ++l) {
+      double dr, di;
+      dv_dparam(g, tau, types, prm, natom, j, l, par / 4, par % 4, &dr, &di);
+#pragma unroll
+      for (int i = 0; i < kMaxCluster; ++i)
+        if (i < c) {
+          const cuDoubleComplex b = u[l + (long)(n0 + i) * nbv];
+          ar[i] += dr * b.x - di * b.y;
+          ai[i] += dr * b.y + di * b.x;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kMaxCluster; ++i)
+      if (i < c) out[j * kMaxCluster + i] = make_cuDoubleComplex(ar[i], ai[i]);
+  }
+}
+
+// M = U_c^H Y (c x c per cluster and parameter; one thread per entry)
+__global__ void k_bulk_cluster_m(int nparam, long nbv, const cuDoubleComplex* __restrict__ h,
+                                 const int* __restrict__ clu,
+                                 const cuDoubleComplex* __restrict__ y,
+                                 cuDoubleComplex* __restrict__ mm) {
+  const int item = blockIdx.x / nparam, par = blockIdx.x % nparam;
+  const int k = clu[3 * item], n0 = clu[3 * item + 1], c = clu[3 * item + 2];
+  const int i = threadIdx.x / kMaxCluster, i2 = threadIdx.x % kMaxCluster;
+  if (i >= c || i2 >= c) return;
+  const cuDoubleComplex* u = h + (long)k * nbv * nbv + (long)(n0 + i) * nbv;
+  const cuDoubleComplex* yy = y + ((long)item * nparam + par) * nbv * kMaxCluster;
+  double re = 0.0, im = 0.0;
+  for (long j = 0; j < nbv; ++j) {
+    const cuDoubleComplex a = u[j], b = yy[j * kMaxCluster + i2];
+    re += a.x * b.x + a.y * b.y;  // conj(a) b
+    im += a.x * b.y - a.y * b.x;
+  }
+  mm[((long)item * nparam + par) * kMaxCluster * kMaxCluster + i * kMaxCluster + i2] =
+      make_cuDoubleComplex(re, im);
+}
+
+// eigenvalues (ascending) of a c x c Hermitian matrix: cyclic Jacobi on its
+// real symmetric embedding [[Re, -Im], [Im, Re]], whose eigenvalues are those
+// of M, each twice
+void hermitian_eigvals(int c, const cuDoubleComplex* m, int ld, double* out) {
+  const int n = 2 * c;
+  std::vector<double> a((size_t)n * n);
+  for (int i = 0; i < c; ++i)
+    for (int j = 0; j < c; ++j) {
+      const double re = 0.5 * (m[i * ld + j].x + m[j * ld + i].x);
+      const double im = 0.5 * (m[i * ld + j].y - m[j * ld + i].y);
+      a[(size_t)i * n + j] = re;
+      a[(size_t)(i + c) * n + (j + c)] = re;
+      a[(size_t)i * n + (j + c)] = -im;
+      a[(size_t)(i + c) * n + j] = im;
+    }
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        tot += a[(size_t)i * n + j] * a[(size_t)i * n + j];
+        if (i != j) off += a[(size_t)i * n + j] * a[(size_t)i * n + j];
+      }
+    if (off <= 1e-30 * tot || off == 0.0) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) /
+                         (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int r = 0; r < n; ++r) {  // columns p, q
+          const double x = a[(size_t)r * n + p], yv = a[(size_t)r * n + q];
+          a[(size_t)r * n + p] = cs * x - sn * yv;
+          a[(size_t)r * n + q] = sn * x + cs * yv;
+        }
+        for (int r = 0; r < n; ++r) {  // rows p, q
+          const double x = a[(size_t)p * n + r], yv = a[(size_t)q * n + r];
+          a[(size_t)p * n + r] = cs * x - sn * yv;
+          a[(size_t)q * n + r] = sn * x + cs * yv;
+        }
+      }
+  }
+  std::vector<double> ev(n);
+  for (int i = 0; i < n; ++i) ev[i] = a[(size_t)i * n + i];
+  std::sort(ev.begin(), ev.end());
+  for (int i = 0; i < c; ++i) out[i] = 0.5 * (ev[2 * i] + ev[2 * i + 1]);
+}
+
 __global__ void k_bulk_grad_sum(const double* __restrict__ partials, long nblocks, int nval,
                                 double* __restrict__ grad) {
   const int i = threadIdx.x;
@@ -413,6 +554,7 @@ int sep_bulk_create(long nbv, const double* g, long natom, const double* tau, co
   b->natom = natom;
   b->nk = nk;
   b->nev = nev;
+  b->nev_cap = nev;
   b->ntype = ntype;
   b->ke_scale = ke_scale;
   auto bail = [&](int r) {
@@ -472,13 +614,75 @@ int sep_bulk_bands_backward(sep_bulk* b, const double* params, const double* dl_
     BK(cudaMemcpyAsync(bands, b->bands, sizeof(double) * b->nk * b->nev, cudaMemcpyDeviceToHost,
                        b->stream));
   }
-  // bands are eV = AUTOEV x eigenvalue: dL/dlambda = AUTOEV dL/dE
-  std::vector<double> g(b->nk * b->nev);
-  for (size_t i = 0; i < g.size(); ++i) g[i] = dl_de[i] * kAutoEv;
+  // Degenerate clusters.  Inside a cluster of equal eigenvalues the
+  // eigenvectors are any basis of its subspace, so sum_n g_n <u_n|dV|u_n>
+  // depends on that basis unless the g_n are equal, and the sorted bands are
+  // not differentiable there.  Each cluster's g is split into its mean, which
+  // enters the density (a trace: basis-free), and the rest, whose part of
+  // the derivative is taken from the cluster's first-order splitting: with
+  // mu the eigenvalues of M = U_c^H dV/dtheta U_c ascending, band n0 + i
+  // moves by +h mu_i for theta + h and by -h mu_{c-1-i} for theta - h, so
+  // the limit of central differences is sum_i g_i (mu_i + mu_{c-1-i}) / 2.
+  // A cluster that reaches past band nev takes its higher bands with g = 0.
+  const long nbv = b->nbv, nk = b->nk, nev = b->nev;
+  std::vector<double> wh((size_t)nk * nbv);
+  BK(cudaMemcpyAsync(wh.data(), b->w, sizeof(double) * wh.size(), cudaMemcpyDeviceToHost,
+                     b->stream));
+  BK(cudaStreamSynchronize(b->stream));
+  struct Cluster {
+    int k, n0, c;
+    std::vector<double> dg;  // g minus the cluster mean
+  };
+  std::vector<Cluster> split;
+  long ncols = nev;  // bands that carry a g (nev, or more where a cluster reaches past it)
+  std::vector<std::vector<double>> gk((size_t)nk);
+  for (long k = 0; k < nk; ++k) {
+    const double* lam = wh.data() + k * nbv;
+    std::vector<double>& gg = gk[(size_t)k];
+    gg.assign((size_t)nbv, 0.0);
+    // bands are eV = AUTOEV x eigenvalue: dL/dlambda = AUTOEV dL/dE
+    for (long n = 0; n < nev; ++n) gg[(size_t)n] = dl_de[k * nev + n] * kAutoEv;
+    long n = 0;
+    while (n < nev) {
+      long e = n + 1;
+      while (e < nbv && std::fabs(lam[e] - lam[e - 1]) <=
+                            1e-10 * std::max(1.0, std::fabs(lam[e])))
+        ++e;
+      const long c = e - n;
+      if (c > 1) {
+        double mean = 0.0;
+        for (long i = n; i < e; ++i) mean += gg[(size_t)i];
+        mean /= (double)c;
+        bool equal = true;
+        for (long i = n; i < e; ++i) equal = equal && gg[(size_t)i] == mean;
+        // a cluster of more than kMaxCluster bands keeps only its mean g (a
+        // basis-free choice, without the splitting term)
+        if (!equal && c <= kMaxCluster) {
+          Cluster cl{(int)k, (int)n, (int)c, std::vector<double>((size_t)c)};
+          for (long i = 0; i < c; ++i) cl.dg[(size_t)i] = gg[(size_t)(n + i)] - mean;
+          split.push_back(std::move(cl));
+        }
+        if (!equal)
+          for (long i = n; i < e; ++i) gg[(size_t)i] = mean;
+        ncols = std::max(ncols, e);
+      }
+      n = e;
+    }
+  }
+  if (ncols > b->nev_cap) {
+    if (b->dlde) cudaFree(b->dlde);
+    b->dlde = nullptr;
+    b->nev_cap = 0;
+    BK(cudaMalloc((void**)&b->dlde, sizeof(double) * (size_t)nk * ncols));
+    b->nev_cap = ncols;
+  }
+  std::vector<double> g((size_t)nk * ncols);
+  for (long k = 0; k < nk; ++k)
+    for (long n = 0; n < ncols; ++n) g[(size_t)(k * ncols + n)] = gk[(size_t)k][(size_t)n];
   BK(cudaMemcpyAsync(b->dlde, g.data(), sizeof(double) * g.size(), cudaMemcpyHostToDevice,
                      b->stream));
   const long n2 = b->nbv * b->nbv;
-  k_bulk_density<<<blocks_for(n2), kThreads, 0, b->stream>>>(b->h, b->dlde, b->nbv, b->nk, b->nev,
+  k_bulk_density<<<blocks_for(n2), kThreads, 0, b->stream>>>(b->h, b->dlde, b->nbv, b->nk, ncols,
                                                               b->wmat);
   BK(cudaGetLastError());
   const unsigned nblk = blocks_for(n2);
@@ -487,9 +691,56 @@ int sep_bulk_bands_backward(sep_bulk* b, const double* params, const double* dl_
   BK(cudaGetLastError());
   k_bulk_grad_sum<<<1, 32, 0, b->stream>>>(b->partials, nblk, (int)(4 * b->ntype), b->grad);
   BK(cudaGetLastError());
-  BK(cudaMemcpyAsync(dl_dparams, b->grad, sizeof(double) * 4 * b->ntype, cudaMemcpyDeviceToHost,
+  const int nparam = (int)(4 * b->ntype);
+  BK(cudaMemcpyAsync(dl_dparams, b->grad, sizeof(double) * nparam, cudaMemcpyDeviceToHost,
                      b->stream));
   BK(cudaStreamSynchronize(b->stream));
+  if (!split.empty()) {
+    const long ns = (long)split.size();
+    if (ns > b->clu_cap) {
+      for (void* q : {(void*)b->clu, (void*)b->cluy, (void*)b->clum})
+        if (q) cudaFree(q);
+      b->clu = nullptr;
+      b->cluy = b->clum = nullptr;
+      b->clu_cap = 0;
+      BK(cudaMalloc((void**)&b->clu, sizeof(int) * 3 * ns));
+      BK(cudaMalloc((void**)&b->cluy,
+                    sizeof(cuDoubleComplex) * (size_t)ns * nparam * nbv * kMaxCluster));
+      BK(cudaMalloc((void**)&b->clum, sizeof(cuDoubleComplex) * (size_t)ns * nparam *
+                                          kMaxCluster * kMaxCluster));
+      b->clu_cap = ns;
+    }
+    std::vector<int> desc((size_t)(3 * ns));
+    for (long i = 0; i < ns; ++i) {
+      desc[(size_t)(3 * i)] = split[(size_t)i].k;
+      desc[(size_t)(3 * i + 1)] = split[(size_t)i].n0;
+      desc[(size_t)(3 * i + 2)] = split[(size_t)i].c;
+    }
+    BK(cudaMemcpyAsync(b->clu, desc.data(), sizeof(int) * desc.size(), cudaMemcpyHostToDevice,
+                       b->stream));
+    k_bulk_cluster_y<<<(unsigned)(ns * nparam), 128, 0, b->stream>>>(
+        b->g, b->tau, b->types, b->params, (int)b->natom, nparam, nbv, b->h, b->clu, b->cluy);
+    BK(cudaGetLastError());
+    k_bulk_cluster_m<<<(unsigned)(ns * nparam), kMaxCluster * kMaxCluster, 0, b->stream>>>(
+        nparam, nbv, b->h, b->clu, b->cluy, b->clum);
+    BK(cudaGetLastError());
+    std::vector<cuDoubleComplex> mh((size_t)ns * nparam * kMaxCluster * kMaxCluster);
+    BK(cudaMemcpyAsync(mh.data(), b->clum, sizeof(cuDoubleComplex) * mh.size(),
+                       cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    std::vector<double> mu(kMaxCluster);
+    for (long i = 0; i < ns; ++i) {
+      const Cluster& cl = split[(size_t)i];
+      for (int par = 0; par < nparam; ++par) {
+        hermitian_eigvals(cl.c, mh.data() + ((size_t)i * nparam + par) * kMaxCluster * kMaxCluster,
+                          kMaxCluster, mu.data());
+        double add = 0.0;
+        for (int r = 0; r < cl.c; ++r)
+          add += cl.dg[(size_t)r] * 0.5 * (mu[(size_t)r] + mu[(size_t)(cl.c - 1 - r)]);
+        dl_dparams[par] += add;
+      }
+    }
+  }
   return SEP_OK;
 }
 
@@ -510,7 +761,8 @@ int sep_bulk_destroy(sep_bulk* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   void* bufs[] = {b->g, b->tau, b->types, b->kpts, b->params, b->v, b->h, b->wmat, b->w,
-                  b->bands, b->dlde, b->partials, b->grad, b->info, b->dwork};
+                  b->bands, b->dlde, b->partials, b->grad, b->info, b->dwork, b->clu,
+                  b->cluy, b->clum};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->sparams) cusolverDnDestroyParams(b->sparams);

@@ -155,3 +155,39 @@ def test_fit_driver_on_the_gpu(tmp_path):
     for name in ("iterations.dat", "output.dat", "bandStruct_0.dat", "kpoints_0.dat",
                  "pot_Cd_0.dat", "best_Se_0_Params.dat"):
         assert (tmp_path / "run" / name).exists(), name
+
+
+@pytest.mark.parametrize("run", ["zb_cdse", "w_cdse"])
+def test_fit_objective_gradient_with_real_weights_matches_central_differences(fits, run):
+    """The fit objective (fit.c:101-122) with its real band weights
+    (fit.c:106-112), whose weights differ inside degenerate clusters (the
+    valence-band top at Gamma): the gradient equals central differences of
+    the objective on the GPU (every parameter) and of the oracle's objective
+    (a0 of each element), h = 1e-6, within 1e-6 of the largest entry."""
+    fit = fits[run]
+    bf = bulk.BulkFit(fit)
+    theta = np.asarray(fit.params, dtype=np.float64)
+    _, grad = bf.objective_and_grad(theta)
+
+    def oracle_objective(th):
+        return np.mean([bo.weighted_mse(
+            bo.bands(c.cell, c.tau, [bulk.fit_atom_params(fit, th, ci, s) for s in c.symbols],
+                     c.kpts, c.max_ke, c.ne, fit.ke_scale), c.exp_bands)
+            for ci, c in enumerate(fit.crystals)])
+
+    h = 1e-6
+    flat = theta.reshape(-1)
+    fd, fd_ref = np.zeros(flat.size), np.full(flat.size, np.nan)
+    for j in range(flat.size):
+        e = np.zeros(flat.size)
+        e[j] = h
+        tp, tm = (flat + e).reshape(theta.shape), (flat - e).reshape(theta.shape)
+        fd[j] = (bf.objective(tp) - bf.objective(tm)) / (2 * h)
+        if j % 4 == 0:
+            fd_ref[j] = (oracle_objective(tp) - oracle_objective(tm)) / (2 * h)
+    g = grad.reshape(-1)
+    scale = np.abs(fd).max()
+    assert np.abs(g - fd).max() < 1e-6 * scale, (g, fd)
+    sel = ~np.isnan(fd_ref)
+    assert np.abs(g - fd_ref)[sel].max() < 1e-6 * scale, (g, fd_ref)
+    bf.close()
