@@ -58,7 +58,7 @@ int sep_device_count(int *count);
  * plans of filter/main.c:58-59.  steps = (dx, dy, dz) in bohr; ekinmax = the
  * kinetic cap in hartree (10.0 in filter/init.c:31; k^2 is pre-scaled by
  * 1/N and capped at ekinmax/N as filter/init.c:125-143).  potl: N doubles or
- * NULL (set later).  Supported axis lengths: 16 18 20 24 32 36 40 48 56 64
+ * NULL (set later).  Supported axis lengths: 14 16 18 20 24 32 36 40 48 56 64
  * 72 80 96 112 128 160 192 256. */
 int sep_ctx_create(const long dims[3], const double steps[3], double ekinmax,
                    const double *potl, int precision, sep_ctx **out);
@@ -439,6 +439,44 @@ int sep_spinor_neighbour_lists(long nx, long ny, long nz, const double *vx, cons
                                const double *vz, long natom, const double *rxyz,
                                const double *vso, double rnlcut2, long nnlc, sep_nlc *nlc,
                                long *nl);
+
+/* ---- the spinor filter program (spinors/filterSpinors/) -------------------
+ * Spinors: 2 ngrid complex values (interleaved re, im doubles), the spin-up
+ * grid then the spin-down grid; H = T + V on each component grid plus the
+ * spin-orbit operator Vso of sep_spinor_vso.  All in FP64, on the context's
+ * grid and local potential.
+ * sep_spinor_set_operator: the neighbour lists (natom x nnlc sep_nlc, nl[a]
+ *   used per atom, every jxyz on the grid), sigma (Gaussian form) or
+ *   flagkb = 1 with elkb (2 natom energies); copied to the device, kept by
+ *   the context until set again.
+ * sep_spinor_hamiltonian: hpsi = H psi for nspinors spinors
+ *   (filterSpinors/hamiltonian.c:8-46).
+ * sep_spinor_energy_range: filterSpinors/energy.c:49-109 from four
+ *   component grids that init_psi draws from the seed -874917403: Emin by
+ *   phi <- normalise(psi - 0.025 H psi), Emax by power iteration, each to a
+ *   relative change of 1e-6 or 500 steps; *vmin = Emin - 0.2 |Emin|,
+ *   *dE = 1.2 Emax - *vmin.
+ * sep_spinor_filter: filterSpinors/filter.c:48-80 for ns start spinors:
+ *   out[s][e] = sum_j (an_re + i an_im)[e][j] psi_j, psi_0 = start[s],
+ *   psi_j = dE_1 H psi_{j-1} - (2 + zn[j-1] + vmin dE_1) psi_{j-1};
+ *   an_re, an_im: ms x nc (ms <= 16); out: ns x ms spinors.
+ * sep_spinor_pipeline: filterSpinors/main.c:84-175 from given start spinors
+ *   (ns x 2 ngrid complex): energy range (dE <= 0: computed, vmin then
+ *   comes from it), coefficients, filter, normalisation, ortho (the Gram
+ *   scheme of sep_ortho on the Hermitian Gram matrix, keeping singular-value
+ *   ratios >= 1e-10 like filterSpinors/ortho.c's zgesvd), Rayleigh-Ritz
+ *   (filterSpinors/Hmat.c), sigma = |H psi - E psi| (energy.c:114-145).
+ *   psi_out (optional): the *mkept Ritz spinors; eval, sige: ns ms entries. */
+int sep_spinor_set_operator(sep_ctx *ctx, long natom, long nnlc, const sep_nlc *nlc,
+                            const long *nl, double sigma, int flagkb, const double *elkb);
+int sep_spinor_hamiltonian(sep_ctx *ctx, const double *psi, double *hpsi, long nspinors);
+int sep_spinor_energy_range(sep_ctx *ctx, double *vmin, double *dE, long *iters);
+int sep_spinor_filter(sep_ctx *ctx, const double *start, long ns, const double *an_re,
+                      const double *an_im, const double *zn, long ms, long nc, double dE_1,
+                      double vmin, double *out);
+int sep_spinor_pipeline(sep_ctx *ctx, const double *start, long ns, const double *el, long ms,
+                        long nc, double vmin, double dE, double *psi_out, double *eval,
+                        double *sige, long *mkept, sep_timing *timing);
 
 #ifdef __cplusplus
 }

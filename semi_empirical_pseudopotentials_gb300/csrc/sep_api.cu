@@ -143,7 +143,8 @@ sep_ctx::~sep_ctx() {
   w_refine.release();
   for (DevBuf* b : {&w_hist, &w_fft, &w_acc, &w_coef, &w_steps, &w_start, &w_out, &w_red,
                     &w_small, &w_states, &w_states2, &w_tmp, &w_solver, &w_gemm, &w_hpsi,
-                    &w_ozA, &w_ozB, &w_ozP, &w_ozE})
+                    &w_ozA, &w_ozB, &w_ozP, &w_ozE, &w_nlc, &w_nl, &w_elkb, &w_so, &w_so2,
+                    &w_so3})
     b->release();
   if (solver) cusolverDnDestroy(solver);
   if (h2d) cudaStreamDestroy(h2d);
@@ -175,7 +176,7 @@ int sep_ctx_create(const long dims[3], const double steps[3], double ekinmax,
       char b[160];
       snprintf(b, sizeof b,
                "sep_ctx_create: axis length %ld has no compiled line pass "
-               "(16 18 20 24 32 36 40 48 56 64 72 80 96 112 128 160 192 256)",
+               "(14 16 18 20 24 32 36 40 48 56 64 72 80 96 112 128 160 192 256)",
                dims[a]);
       return arg_fail(b);
     }

@@ -81,14 +81,15 @@ void DevBuf::release() {
 }
 
 bool length_supported(int L) {
-  static const int ok[] = {16, 18, 20, 24, 32, 36, 40, 48, 56, 64, 72, 80, 96, 112, 128, 160,
+  static const int ok[] = {14, 16, 18, 20, 24, 32, 36, 40, 48, 56, 64, 72, 80, 96, 112, 128, 160,
                            192, 256};
   for (int v : ok)
     if (v == L) return true;
   return false;
 }
 
-namespace {
+// helpers shared with sep_spinor_path.cu (declared in sep_ctx_detail.cuh)
+namespace detail {
 
 void drop_graphs(sep_ctx* c) {
   for (auto& g : c->graphs)
@@ -536,7 +537,8 @@ int rotate_rows(sep_ctx* c, double* d_psi, long long m, long long k, const doubl
   return oz_check(c);
 }
 
-}  // namespace
+}  // namespace detail
+using namespace detail;
 
 int release_filter_workspace_if_short(sep_ctx* c, size_t need) {
   if (free_device_bytes() >= need || c->batch_holds > 0) return kOk;

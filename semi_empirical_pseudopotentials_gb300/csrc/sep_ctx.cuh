@@ -85,6 +85,14 @@ struct sep_ctx {
   sep::GridDev<float> g32;
   // workspace
   sep::DevBuf w_refine;  // psi and its residual directions (refine_device)
+  // spin-orbit operator of the spinor path (sep_spinor_set_operator): the
+  // neighbour lists (nlc_st layout), their counts and the Kleinman-Bylander
+  // energies on the device; w_so / w_so2 / w_so3: Vso psi and spinor blocks
+  long so_natom = 0, so_nnlc = 0;
+  double so_sigma = 0.0;
+  int so_flagkb = 0;
+  bool so_ready = false;
+  sep::DevBuf w_nlc, w_nl, w_elkb, w_so, w_so2, w_so3;
   sep::DevBuf w_hist, w_fft, w_acc, w_coef, w_steps, w_start, w_out, w_red, w_small,
       w_states, w_states2, w_tmp, w_solver, w_gemm, w_hpsi, w_ozA, w_ozB, w_ozP, w_ozE;
   std::vector<sep::FilterGraph> graphs;

@@ -48,6 +48,7 @@ template <typename T> struct PassIO {
   cx<T>* data = nullptr;
   const cx<T>* src = nullptr;
   const cx<T>* psi_in = nullptr;
+  const cx<T>* extra = nullptr;  // x-pass epilogue: added to T psi (the spin-orbit term)
   cx<T>* psi_out = nullptr;
   T alpha = T(1), beta = T(0);
   const T* coefs = nullptr;  // device (alpha, beta) per step

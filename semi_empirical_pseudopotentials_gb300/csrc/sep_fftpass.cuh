@@ -37,6 +37,7 @@ template <typename T> struct PassArgs {
   cx<T>* data;            // transformed in place
   const cx<T>* src;       // kFwd: read from here instead of data when not null
   const cx<T>* psi_in;    // epilogue: previous state (null: no V and no beta term)
+  const cx<T>* extra;     // epilogue: added to T psi before the alpha scale (null: none)
   cx<T>* psi_out;         // epilogue: new state
   const T* pot;           // epilogue: V on the grid (shared by the batch)
   const cx<T>* tw;        // exp(-2 pi i m / L), m < L, for this axis
@@ -57,6 +58,7 @@ template <typename T> struct PassArgs {
 template <int L> struct Split;
 #define SEP_SPLIT(L_, A_, B_) \
   template <> struct Split<L_> { static constexpr int n1 = A_, n2 = B_; };
+SEP_SPLIT(14, 2, 7)
 SEP_SPLIT(16, 4, 4)
 SEP_SPLIT(18, 6, 3)
 SEP_SPLIT(20, 4, 5)
@@ -334,6 +336,7 @@ line_pass(PassArgs<T> a) {
         const long long lb = base0 + line * lstride;          // offset in the batch array
         const long long gb = lb % N;                          // offset in one grid
         const C* pin = a.psi_in ? a.psi_in + lb : nullptr;
+        const C* pex = a.extra ? a.extra + lb : nullptr;
         C* pout = a.psi_out + lb;
         const T* pv = a.pot + gb;
 #pragma unroll
@@ -341,7 +344,9 @@ line_pass(PassArgs<T> a) {
           const int x = n1 + N1 * n2;
           const C p = pin ? pin[x] : mk<T>(T(0), T(0));
           const T v = pv[x];
-          const C o = newton_epi<T>(va[r][n2], v, p, alpha, beta);
+          C u = va[r][n2];
+          if (pex) u = mk<T>(u.x + pex[x].x, u.y + pex[x].y);
+          const C o = newton_epi<T>(u, v, p, alpha, beta);
           pout[x] = o;
           va[r][n2] = o;
         }

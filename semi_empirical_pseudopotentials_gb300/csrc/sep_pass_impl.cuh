@@ -54,7 +54,7 @@ cudaError_t launch_variant<SEP_T, SEP_V>(int axis, int mode, int L, const PassAr
   switch (L) {
 #define SEP_CASE(LL) \
   case LL: return launch_len<SEP_T, LL, SEP_V>(axis, mode, a, B, s);
-    SEP_CASE(16) SEP_CASE(18) SEP_CASE(20) SEP_CASE(24) SEP_CASE(32) SEP_CASE(36)
+    SEP_CASE(14) SEP_CASE(16) SEP_CASE(18) SEP_CASE(20) SEP_CASE(24) SEP_CASE(32) SEP_CASE(36)
     SEP_CASE(40) SEP_CASE(48) SEP_CASE(56) SEP_CASE(64) SEP_CASE(72) SEP_CASE(80)
     SEP_CASE(96) SEP_CASE(112) SEP_CASE(128) SEP_CASE(160) SEP_CASE(192) SEP_CASE(256)
 #undef SEP_CASE
@@ -71,6 +71,7 @@ cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
   a.data = io.data;
   a.src = io.src;
   a.psi_in = io.psi_in;
+  a.extra = io.extra;
   a.psi_out = io.psi_out;
   a.coefs = io.coefs;
   a.step = io.step;

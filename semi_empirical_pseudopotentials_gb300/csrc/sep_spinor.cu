@@ -70,6 +70,7 @@ __device__ __forceinline__ void atomic_add(double* p, C2 v) {
 }
 
 // sums index: 0 y11 up, 1 y10 up, 2 y1_1 up, 3 y11 dn, 4 y10 dn, 5 y1_1 dn
+// grid: x = atom, y = spinor of the batch (spinors 4 ngrid doubles apart)
 __global__ void __launch_bounds__(kT) k_vso_gauss(const double* __restrict__ psi, long ngrid,
                                                   long nnlc, const sep_nlc* __restrict__ nlc,
                                                   const long* __restrict__ nl, double tmp,
@@ -77,6 +78,8 @@ __global__ void __launch_bounds__(kT) k_vso_gauss(const double* __restrict__ psi
   __shared__ double sr[kT], sr2[kT], svr[kT];
   __shared__ C2 sx[6][kT];
   const long a = blockIdx.x;
+  psi += (size_t)blockIdx.y * 4 * (size_t)ngrid;
+  out += (size_t)blockIdx.y * 4 * (size_t)ngrid;
   const long n = nl[a];
   const sep_nlc* base = nlc + a * nnlc;
   const int tid = threadIdx.x;
@@ -148,6 +151,8 @@ __global__ void __launch_bounds__(kT) k_vso_kb(const double* __restrict__ psi, l
   __shared__ double red[kT / 32][24];
   __shared__ double proj[24];
   const long a = blockIdx.x;
+  psi += (size_t)blockIdx.y * 4 * (size_t)ngrid;
+  out += (size_t)blockIdx.y * 4 * (size_t)ngrid;
   const long n = nl[a];
   const sep_nlc* base = nlc + a * nnlc;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -222,6 +227,26 @@ __global__ void __launch_bounds__(kT) k_vso_kb(const double* __restrict__ psi, l
 
 }  // namespace
 
+namespace sep {
+// Vso on nsp spinors (4 ngrid doubles apart) into psinl (zeroed first), on st;
+// the arguments are already checked.  nsp <= 65535.
+cudaError_t spinor_vso_launch(const double* psi, long ngrid, long nsp, long natom, long nnlc,
+                              const sep_nlc* nlc, const long* nl, double sigma, double dv,
+                              int flagkb, const double* elkb, double* psinl, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(psinl, 0, sizeof(double) * 4 * (size_t)ngrid * nsp, st);
+  if (e != cudaSuccess || natom == 0) return e;
+  const dim3 grid((unsigned)natom, (unsigned)nsp);
+  if (flagkb) {
+    k_vso_kb<<<grid, kT, 0, st>>>(psi, ngrid, nnlc, nlc, nl, elkb, natom, dv, psinl);
+  } else {
+    const double tmp = 0.5 / sqrt(kTwoPi * (sigma * sigma)) * dv;  // hamiltonian.c:89
+    const double sigma_1 = sqrt(0.5) / sigma;                       // init.c:97
+    k_vso_gauss<<<grid, kT, 0, st>>>(psi, ngrid, nnlc, nlc, nl, tmp, sigma_1, psinl);
+  }
+  return cudaGetLastError();
+}
+}  // namespace sep
+
 extern "C" {
 
 int sep_spinor_vso_dev(const double* psi, long ngrid, long natom, long nnlc, const sep_nlc* nlc,
@@ -231,16 +256,8 @@ int sep_spinor_vso_dev(const double* psi, long ngrid, long natom, long nnlc, con
       (flagkb && !elkb) || (!flagkb && !(sigma > 0.0)))
     return fail(SEP_ERR_ARG, "sep_spinor_vso: bad arguments");
   cudaStream_t st = (cudaStream_t)cuda_stream;
-  SK(cudaMemsetAsync(psinl, 0, sizeof(double) * 4 * ngrid, st));
-  if (natom == 0) return SEP_OK;
-  if (flagkb) {
-    k_vso_kb<<<(unsigned)natom, kT, 0, st>>>(psi, ngrid, nnlc, nlc, nl, elkb, natom, dv, psinl);
-  } else {
-    const double tmp = 0.5 / sqrt(kTwoPi * (sigma * sigma)) * dv;  // hamiltonian.c:89
-    const double sigma_1 = sqrt(0.5) / sigma;                       // init.c:97
-    k_vso_gauss<<<(unsigned)natom, kT, 0, st>>>(psi, ngrid, nnlc, nlc, nl, tmp, sigma_1, psinl);
-  }
-  SK(cudaGetLastError());
+  SK(sep::spinor_vso_launch(psi, ngrid, 1, natom, nnlc, nlc, nl, sigma, dv, flagkb, elkb, psinl,
+                            st));
   return SEP_OK;
 }
 

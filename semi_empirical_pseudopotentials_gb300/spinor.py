@@ -12,13 +12,17 @@ this layout.
 * ``nonlocal_potential(psi, nlc, nl, sigma, dv)``: the Gaussian form,
   filterSpinors/hamiltonian.c:81-190;
 * ``nonlocal_potential_kb(psi, nlc, nl, elkb, dv)``: the Kleinman-Bylander
-  form, filterSpinors/hamiltonian.c:193-401.
+  form, filterSpinors/hamiltonian.c:193-401;
+* ``SpinorPath(ctx, nlc, nl, sigma=..., elkb=...)``: the spinor filter
+  program on a context's grid and potential -- the spinor Hamiltonian, its
+  energy range, the Newton filter with complex coefficients and the whole
+  pipeline (filterSpinors/main.c:84-175).
 """
 import ctypes as C
 
 import numpy as np
 
-from .binding import _check, lib
+from .binding import Timing, _check, lib
 
 NLC_DTYPE = np.dtype([("jxyz", "<i8"), ("y10", "<c16"), ("y11", "<c16"), ("y1_1", "<c16"),
                       ("Vs0G1", "<f8"), ("Vs0G_2", "<f8"), ("r", "<f8"), ("r2_1", "<f8"),
@@ -86,3 +90,92 @@ def nonlocal_potential(psi, nlc, nl, sigma, dv):
 def nonlocal_potential_kb(psi, nlc, nl, elkb, dv):
     """Vso psi, Kleinman-Bylander form (filterSpinors/hamiltonian.c:193-401)."""
     return _apply(psi, nlc, nl, 1.0, dv, 1, elkb)
+
+
+class SpinorPath:
+    """The spinor filter program on the grid and local potential of a
+    binding.Context (FP64).  Spinors are complex arrays of 2 ngrid values."""
+
+    def __init__(self, ctx, nlc, nl, sigma=None, elkb=None):
+        self.ctx = ctx
+        nlc = np.ascontiguousarray(nlc, dtype=NLC_DTYPE)
+        nl = np.ascontiguousarray(nl, dtype=np.int64)
+        natom, nnlc = nlc.shape
+        flagkb = elkb is not None
+        el = None
+        if flagkb:
+            el = np.ascontiguousarray(elkb, dtype=np.float64)
+            if el.shape != (2 * natom,):
+                raise ValueError("elkb has 2 natom entries")
+        dp = C.POINTER(C.c_double)
+        L = lib()
+        L.sep_spinor_set_operator.argtypes = [C.c_void_p, C.c_long, C.c_long, C.c_void_p,
+                                              C.c_void_p, C.c_double, C.c_int, C.c_void_p]
+        _check(L.sep_spinor_set_operator(ctx.h, natom, nnlc, nlc.ctypes.data, nl.ctypes.data,
+                                         float(sigma or 0.0), int(flagkb),
+                                         el.ctypes.data if el is not None else None))
+        self._keep = (nlc, nl, el)
+        self.n = ctx.ngrid
+
+    def _spinors(self, psi):
+        z = np.ascontiguousarray(psi, dtype=np.complex128)
+        return z.reshape(-1, 2 * self.n)
+
+    def hamiltonian(self, psi):
+        """H psi (filterSpinors/hamiltonian.c:8-46), one or more spinors."""
+        z = self._spinors(psi)
+        out = np.empty_like(z)
+        L = lib()
+        L.sep_spinor_hamiltonian.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long]
+        _check(L.sep_spinor_hamiltonian(self.ctx.h, z.ctypes.data, out.ctypes.data, z.shape[0]))
+        return out.reshape(np.shape(psi))
+
+    def energy_range(self):
+        """(vmin, dE, iterations) of filterSpinors/energy.c:49-109."""
+        vmin, dE, it = C.c_double(), C.c_double(), C.c_long()
+        L = lib()
+        L.sep_spinor_energy_range.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _check(L.sep_spinor_energy_range(self.ctx.h, C.byref(vmin), C.byref(dE), C.byref(it)))
+        return vmin.value, dE.value, it.value
+
+    def filter(self, start, an, zn, dE_1, vmin):
+        """filterSpinors/filter.c:48-80: [ns, ms, 2 ngrid] from [ns, 2 ngrid]
+        start spinors and complex coefficients an [ms, nc]."""
+        st = self._spinors(start)
+        an = np.asarray(an, dtype=np.complex128)
+        ar = np.ascontiguousarray(an.real)
+        ai = np.ascontiguousarray(an.imag)
+        zn = np.ascontiguousarray(zn, dtype=np.float64)
+        ms, nc = ar.shape
+        out = np.empty((st.shape[0], ms, 2 * self.n), dtype=np.complex128)
+        L = lib()
+        L.sep_spinor_filter.argtypes = [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_long, C.c_long, C.c_double,
+                                        C.c_double, C.c_void_p]
+        _check(L.sep_spinor_filter(self.ctx.h, st.ctypes.data, st.shape[0], ar.ctypes.data,
+                                   ai.ctypes.data, zn.ctypes.data, ms, nc, float(dE_1),
+                                   float(vmin), out.ctypes.data))
+        return out
+
+    def pipeline(self, start, el, nc, vmin=0.0, dE=0.0, want_psi=False):
+        """filterSpinors/main.c:84-175 from given start spinors [ns, 2 ngrid]."""
+        st = self._spinors(start)
+        el = np.ascontiguousarray(el, dtype=np.float64)
+        ns, ms = st.shape[0], len(el)
+        m = ns * ms
+        ev, sg = np.zeros(m), np.zeros(m)
+        psi = np.empty((m, 2 * self.n), dtype=np.complex128) if want_psi else None
+        k = C.c_long()
+        t = Timing()
+        L = lib()
+        L.sep_spinor_pipeline.argtypes = [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p, C.c_long,
+                                          C.c_long, C.c_double, C.c_double, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _check(L.sep_spinor_pipeline(self.ctx.h, st.ctypes.data, ns, el.ctypes.data, ms, int(nc),
+                                     float(vmin), float(dE),
+                                     psi.ctypes.data if psi is not None else None,
+                                     ev.ctypes.data, sg.ctypes.data, C.byref(k), C.byref(t)))
+        kk = k.value
+        return {"eval": ev[:kk], "sigma": sg[:kk], "mkept": kk,
+                "psi": None if psi is None else psi[:kk],
+                "timing": {f: getattr(t, f) for f, _ in Timing._fields_}}

@@ -47,7 +47,7 @@ def test_hamiltonian_matches_reference_output(golden):
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("dims", [(16, 18, 20), (36, 36, 36), (32, 40, 48), (64, 64, 64),
+@pytest.mark.parametrize("dims", [(16, 18, 20), (14, 20, 14), (36, 36, 36), (32, 40, 48), (64, 64, 64),
                                   (56, 72, 80), (96, 112, 128), (128, 128, 128),
                                   (192, 160, 24), (256, 192, 16), (16, 24, 256),
                                   (160, 16, 192)])
