@@ -18,6 +18,8 @@
 #ifndef SEP_GB300_H
 #define SEP_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -279,6 +281,28 @@ int sep_subspace_gemm_dev(sep_ctx *ctx, const double *A, const double *B, long m
 /* out (m x w) = W (m x k) X (k x w), host row-major.  Uses the context's mode. */
 int sep_subspace_rotate(sep_ctx *ctx, const double *W, const double *X, long m, long k, long w,
                         double *out);
+
+/* ---- dense symmetric eigensolver -------------------------------------------
+ * The eigen-decompositions of ortho (filter/ortho.c:11-52, where the reference
+ * calls dgesvd) and Rayleigh-Ritz (filter/Hmat.c:11-86, dsyev) run on the
+ * library's own FP64 solver or on cuSOLVER's syevd.  The library's solver:
+ * Householder tridiagonalisation in one cooperative kernel, divide and
+ * conquer on the tridiagonal (QL leaves of 8 rows, deflation, secular roots
+ * by bisection, Loewner-corrected vectors), back-transformation; no library
+ * call.  mode 1: the library's solver, 0: cuSOLVER (default). */
+int sep_ctx_set_eigensolver(sep_ctx *ctx, int mode);
+/* w (n) ascending and v (n x n, column-major: v[i + j n] is component i of
+ * eigenvector j) of the symmetric n x n matrix a (host arrays, n <= 16384),
+ * on the calling thread's current device with the library's solver. */
+int sep_eigh(const double *a, long n, double *w, double *v);
+/* The same on device arrays: a_dev (n x n) becomes the eigenvectors, w_dev
+ * the eigenvalues; work_dev holds sep_eigh_work_bytes(n) bytes.  Returns
+ * after the stream has reached its end (the merges sort on the host).
+ * stage_ms (3 doubles, may be NULL): device times of the tridiagonalisation,
+ * the divide and conquer and the back-transformation. */
+size_t sep_eigh_work_bytes(long n);
+int sep_eigh_dev(double *a_dev, long n, double *w_dev, double *work_dev, void *cuda_stream,
+                 double *stage_ms);
 
 /* ---- measurement --------------------------------------------------------
  * Average device time (ms, CUDA events on the context stream) of one launch

@@ -97,6 +97,7 @@ def lib():
         L.sep_ctx_set_fusion.argtypes = [vp, C.c_int]
         L.sep_ctx_set_refine.argtypes = [vp, C.c_int]
         L.sep_ctx_set_polish.argtypes = [vp, C.c_long, C.c_double]
+        L.sep_ctx_set_eigensolver.argtypes = [vp, C.c_int]
         L.sep_subspace_gemm.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, C.c_double,
                                         C.c_int, dp]
         L.sep_subspace_rotate.argtypes = [vp, dp, dp, C.c_long, C.c_long, C.c_long, dp]
@@ -387,6 +388,12 @@ class Context:
         """FP64 polish of the window's Ritz pairs in pipeline(): nc Newton steps of
         one wide Gaussian at the window centre (0 = off), guard in hartree."""
         _check(lib().sep_ctx_set_polish(self.h, int(nc), float(guard)))
+
+    def set_eigensolver(self, mode):
+        """Dense symmetric eigensolves of ortho and Rayleigh-Ritz: the library's
+        own solver ("native" or 1) or cuSOLVER ("cusolver" or 0)."""
+        m = {"native": 1, "cusolver": 0}.get(mode, mode)
+        _check(lib().sep_ctx_set_eigensolver(self.h, int(m)))
 
     def set_fusion(self, enable):
         """Fused xy plane pass for complex64 Newton steps (nx = ny in 64/96/128)."""

@@ -11,6 +11,7 @@
 
 #include "../../include/sep_gb300.h"
 #include "sep_ctx.cuh"
+#include "sep_eigh.cuh"
 
 namespace sep {
 const char* last_error();
@@ -144,7 +145,7 @@ sep_ctx::~sep_ctx() {
   for (DevBuf* b : {&w_hist, &w_fft, &w_acc, &w_coef, &w_steps, &w_start, &w_out, &w_red,
                     &w_small, &w_states, &w_states2, &w_tmp, &w_solver, &w_gemm, &w_hpsi,
                     &w_ozA, &w_ozB, &w_ozP, &w_ozE, &w_nlc, &w_nl, &w_elkb, &w_so, &w_so2,
-                    &w_so3})
+                    &w_so3, &w_eigh})
     b->release();
   if (solver) cusolverDnDestroy(solver);
   if (h2d) cudaStreamDestroy(h2d);
@@ -640,6 +641,69 @@ int sep_ctx_set_polish(sep_ctx* c, long nc, double guard) {
     return arg_fail("sep_ctx_set_polish: nc in {0} or [2, 8192] and a finite guard >= 0");
   c->polish_nc = nc;
   c->polish_guard = guard;
+  return kOk;
+}
+
+int sep_ctx_set_eigensolver(sep_ctx* c, int mode) {
+  if (!c || mode < 0 || mode > 1) return arg_fail("sep_ctx_set_eigensolver: mode 0 or 1");
+  c->eigensolver = mode;
+  return kOk;
+}
+
+int sep_eigh(const double* a, long n, double* w, double* v) {
+  if (!a || !w || !v || n < 1 || n > 16384) return arg_fail("sep_eigh: bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    set_error("sep_eigh: no CUDA device");
+    return kErrNoDevice;
+  }
+  const size_t nn = (size_t)n * n;
+  double *dA = nullptr, *dw = nullptr, *work = nullptr;
+  cudaStream_t s = nullptr;
+  auto done = [&](int r) {
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(dA);
+    cudaFree(dw);
+    cudaFree(work);
+    if (s) cudaStreamDestroy(s);
+    return r;
+  };
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&dA, sizeof(double) * nn) != cudaSuccess ||
+      cudaMalloc(&dw, sizeof(double) * n) != cudaSuccess ||
+      cudaMalloc(&work, sizeof(double) * eigh::work_doubles(n)) != cudaSuccess)
+    return done(cuda_fail(cudaGetLastError(), "sep_eigh: allocation", __LINE__));
+  cudaError_t e = cudaMemcpyAsync(dA, a, sizeof(double) * nn, cudaMemcpyHostToDevice, s);
+  int bad = 0;
+  if (e == cudaSuccess) e = eigh::solve(dA, (int)n, dw, work, s, &bad);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(w, dw, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(v, dA, sizeof(double) * nn, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return done(cuda_fail(e, "sep_eigh", __LINE__));
+  if (bad) {
+    set_error("sep_eigh: the QL iteration of a leaf did not converge");
+    return done(kErrSolver);
+  }
+  return done(kOk);
+}
+
+size_t sep_eigh_work_bytes(long n) {
+  return n < 1 ? 0 : sizeof(double) * eigh::work_doubles(n);
+}
+
+int sep_eigh_dev(double* a_dev, long n, double* w_dev, double* work_dev, void* cuda_stream,
+                 double* stage_ms) {
+  if (!a_dev || !w_dev || !work_dev || n < 1 || n > 16384)
+    return arg_fail("sep_eigh_dev: bad argument");
+  int bad = 0;
+  cudaError_t e = eigh::solve(a_dev, (int)n, w_dev, work_dev,
+                              static_cast<cudaStream_t>(cuda_stream), &bad, stage_ms);
+  if (e != cudaSuccess) return cuda_fail(e, "sep_eigh_dev", __LINE__);
+  if (bad) {
+    set_error("sep_eigh_dev: the QL iteration of a leaf did not converge");
+    return kErrSolver;
+  }
   return kOk;
 }
 

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "sep_ctx.cuh"
+#include "sep_eigh.cuh"
 #include "sep_ozaki.cuh"
 
 namespace sep {
@@ -409,8 +410,19 @@ int precond_real(sep_ctx* c, double* d_x, long long m, double shift) {
   return kOk;
 }
 
-// symmetric eigen-decomposition in place (column-major == row-major); w ascending
+// symmetric eigen-decomposition in place (column-major == row-major); w ascending.
+// c->eigensolver 1: the library's own solver (sep_eigh.cu); 0: cuSOLVER syevd.
 int syevd(sep_ctx* c, double* d_a, long long m, double* d_w) {
+  if (c->eigensolver == 1) {
+    RET(grow(c, c->w_eigh, sizeof(double) * eigh::work_doubles(m)));
+    int bad = 0;
+    CK(eigh::solve(d_a, (int)m, d_w, c->w_eigh.as<double>(), c->stream, &bad));
+    if (bad) {
+      set_error("eigensolver: the QL iteration of a leaf did not converge");
+      return kErrSolver;
+    }
+    return kOk;
+  }
   int lwork = 0;
   CKS(cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER,
                                   (int)m, d_a, (int)m, d_w, &lwork));

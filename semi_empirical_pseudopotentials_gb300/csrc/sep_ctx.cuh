@@ -77,6 +77,7 @@ struct sep_ctx {
   long polish_nc = 0;     // FP64 polish of the window's Ritz pairs in sep_pipeline (0 = off)
   double polish_guard = 0.01;  // hartree beyond the target window included in the polish
   int subspace_tc = 1;  // subspace contractions on the tensor cores (1) or the FP64 pipe (0)
+  int eigensolver = 0;  // dense symmetric eigensolves: the library's own (1) or cuSOLVER (0)
   int fuse_xy = 1;      // complex64 Newton steps with the fused xy plane pass when it applies
   bool xy_ready = false;
   int batch_holds = 0;  // batches whose graph points at the filter workspace
@@ -93,6 +94,7 @@ struct sep_ctx {
   int so_flagkb = 0;
   bool so_ready = false;
   sep::DevBuf w_nlc, w_nl, w_elkb, w_so, w_so2, w_so3;
+  sep::DevBuf w_eigh;  // workspace of the symmetric eigensolver
   sep::DevBuf w_hist, w_fft, w_acc, w_coef, w_steps, w_start, w_out, w_red, w_small,
       w_states, w_states2, w_tmp, w_solver, w_gemm, w_hpsi, w_ozA, w_ozB, w_ozP, w_ozE;
   std::vector<sep::FilterGraph> graphs;
