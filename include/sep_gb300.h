@@ -289,7 +289,7 @@ int sep_subspace_rotate(sep_ctx *ctx, const double *W, const double *X, long m, 
  * Householder tridiagonalisation in one cooperative kernel, divide and
  * conquer on the tridiagonal (QL leaves of 8 rows, deflation, secular roots
  * by bisection, Loewner-corrected vectors), back-transformation; no library
- * call.  mode 1: the library's solver, 0: cuSOLVER (default). */
+ * call.  mode 1 (default): the library's solver, 0: cuSOLVER's syevd. */
 int sep_ctx_set_eigensolver(sep_ctx *ctx, int mode);
 /* w (n) ascending and v (n x n, column-major: v[i + j n] is component i of
  * eigenvector j) of the symmetric n x n matrix a (host arrays, n <= 16384),

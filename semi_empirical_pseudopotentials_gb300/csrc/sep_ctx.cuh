@@ -77,7 +77,7 @@ struct sep_ctx {
   long polish_nc = 0;     // FP64 polish of the window's Ritz pairs in sep_pipeline (0 = off)
   double polish_guard = 0.01;  // hartree beyond the target window included in the polish
   int subspace_tc = 1;  // subspace contractions on the tensor cores (1) or the FP64 pipe (0)
-  int eigensolver = 0;  // dense symmetric eigensolves: the library's own (1) or cuSOLVER (0)
+  int eigensolver = 1;  // dense symmetric eigensolves: the library's own (1, default) or cuSOLVER (0)
   int fuse_xy = 1;      // complex64 Newton steps with the fused xy plane pass when it applies
   bool xy_ready = false;
   int batch_holds = 0;  // batches whose graph points at the filter workspace

@@ -9,20 +9,20 @@
 //  1. Householder tridiagonalisation A = Q T Q^T (LAPACK's dsytd2 scheme:
 //     reflector H_k = I - tau v v^T with v[k+1] = 1 annihilates column k below
 //     the subdiagonal; p = tau A22 v, w = p - (tau/2)(p.v) v,
-//     A22 -= v w^T + w v^T).  One cooperative kernel runs all steps: per step
-//     one pass computes p (a warp per row), a grid barrier, one pass applies
-//     the rank-2 update, and the warp that owns the next row forms the next
-//     reflector from it right after updating it; a second grid barrier.  The
-//     rows of a step are spread over all blocks: on this part the FP64 pipe
-//     (about 2 FMAs per clock per SM) is the scarce resource.
+//     A22 -= v w^T + w v^T).  One cooperative kernel runs all steps with one
+//     grid barrier per step: each block forms the next reflector itself from
+//     the next row updated on the fly, then one pass over the trailing rows
+//     applies the update and accumulates the next step's p.  The rows of a
+//     step are spread over all blocks: on this part the FP64 pipe (about 2
+//     FMAs per clock per SM) is the scarce resource.
 //  2. The eigenpairs of T by divide and conquer (Cuppen's method): T is
 //     split recursively into leaves of at most 8 rows, T = diag(T1, T2) +
 //     rho u u^T at each split; the leaves are solved by the implicit QL
 //     iteration with Wilkinson shifts (EISPACK tql2, one warp per leaf);
 //     each merge deflates negligible and near-equal components (Givens
 //     rotations), finds the roots of the secular equation
-//     1 + rho sum z_i^2 / (d_i - lambda) = 0 by bisection in the distance to
-//     the nearer pole, recomputes z from the roots (Loewner's formula, which
+//     1 + rho sum z_i^2 / (d_i - lambda) = 0 by safeguarded Newton steps in
+//     the distance to the nearer pole (bisection of the bracket as fallback), recomputes z from the roots (Loewner's formula, which
 //     keeps the merged eigenvectors orthogonal) and forms the eigenvectors
 //     with one product per merge.  The deflation scan and the sorting run on
 //     the host (O(n) per level).
@@ -71,122 +71,176 @@ __device__ __forceinline__ double warp_prod(double v) {
 
 // ---- 1. tridiagonalisation -------------------------------------------------
 
-// the reflector of step s from row s of A (A[s][s+1..n) = column s below the
-// diagonal): alpha = A[s][s+1], x = A[s][s+2..n); dlarfg's conventions.
-// Called by one whole warp; writes v_s (row s of Vh, v[s+1] = 1), d[s],
-// e[s] (= beta) and tau[s].
-__device__ void house(const double* __restrict__ A, int n, int s, double* d, double* e,
-                      double* tau, double* Vh) {
-  const int lane = threadIdx.x & 31;
-  const double* row = A + (size_t)s * n;
-  double* v = Vh + (size_t)s * n;
-  double amax = 0.0;
-  for (int j = s + 2 + lane; j < n; j += 32) amax = fmax(amax, fabs(row[j]));
-  amax = warp_max(amax);
-  double xnorm = 0.0;
-  if (amax > 0.0) {
-    double ss = 0.0;
-    for (int j = s + 2 + lane; j < n; j += 32) {
-      const double q = row[j] / amax;
-      ss += q * q;
-    }
-    xnorm = amax * sqrt(warp_sum(ss));
-  }
-  const double alpha = row[s + 1];
-  double beta, t, scal;
-  if (xnorm == 0.0) {
-    beta = alpha;
-    t = 0.0;
-    scal = 0.0;
-  } else {
-    beta = -copysign(hypot(alpha, xnorm), alpha);
-    t = (beta - alpha) / beta;
-    scal = 1.0 / (alpha - beta);
-  }
-  for (int j = s + 2 + lane; j < n; j += 32) v[j] = row[j] * scal;
-  if (lane == 0) {
-    v[s + 1] = 1.0;
-    d[s] = row[s];
-    e[s] = beta;
-    tau[s] = t;
-  }
-  __syncwarp();
+// Block-wide reductions (blockDim.x = kT) through red[kT / 32].
+__device__ __forceinline__ double block_max(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double m = 0.0;
+  for (int q = 0; q < kT / 32; ++q) m = fmax(m, red[q]);
+  return m;
+}
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double m = 0.0;
+  for (int q = 0; q < kT / 32; ++q) m += red[q];
+  return m;
 }
 
-// Rows are owned by warps: row r by warp (r % G, (r / G) % 8) of block
-// r % G, so that consecutive rows sit on different SMs and every step's
-// FP64 work spreads over the whole grid.  part: 2 x gridDim.x partial sums
-// of p.v (deterministic order).
+// One grid barrier per step.  Every block keeps the current reflector v_k
+// in shared memory (vk) and builds the next one itself: row k+1 after step
+// k's rank-2 update, x_j = A[k+1][j] - (v_{k+1} p_j + u_{k+1} v_j), is
+// formed on the fly from the stored row (rows and columns <= k+1 are not
+// written back: later steps read only the trailing block), and the
+// reflector of x (dlarfg's conventions, scaled by max |x| against
+// over/underflow) goes to vn.  One pass over the trailing rows i >= k+2 then
+// applies step k's update, A[i][j] -= v_i p_j + u_i v_j with
+// u_i = p_i - 2 c v_i and c = tau_k (p.v) / 2, and accumulates step k+1's
+// p_i = tau_{k+1} sum_j A[i][j] vn_j from the updated values.  Every block
+// computes the reflectors identically; block 0 stores them (Vh, tau, d, e).
+// Rows are owned by warps: row r by warp (r % G, (r / G) % 8), so that
+// consecutive rows sit on different SMs.  p: 2 x n (by step parity);
+// part: 2 x gridDim.x partial sums of p.v (deterministic order).
 __global__ void __launch_bounds__(kT) k_sytrd(double* __restrict__ A, int n, double* d,
                                               double* e, double* tau, double* Vh,
-                                              double* __restrict__ p, double* part) {
+                                              double* __restrict__ pbuf, double* part) {
   cg::grid_group grid = cg::this_grid();
-  __shared__ double sred[kT / 32];
-  __shared__ double spv;
+  extern __shared__ double sm[];
+  double* vbuf = sm;         // 2 x n: the reflectors of steps k (k & 1) and k + 1
+  double* red = sm + 2 * n;  // kT / 32
+  __shared__ double sc[4];   // tau, beta, scale of the reflector being built
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int W = gridDim.x * (kT / 32);
-  const int gw = blockIdx.x + gridDim.x * wib;  // rows gw, gw + W, ...
+  const int gw = blockIdx.x + gridDim.x * wib;
   auto first = [&](int r0) { return r0 + ((gw - r0) % W + W) % W; };
-  if (n >= 3 && gw == 0) house(A, n, 0, d, e, tau, Vh);
+  // the reflector of step s from x[j] (j in [s+1, n), held in vn): vn <- v
+  auto reflector = [&](int s, double* vn) {
+    // |x| unscaled; scaled by max |x| only when the sum of squares under- or
+    // overflows
+    double ss = 0.0;
+    for (int j = s + 2 + threadIdx.x; j < n; j += kT) ss = fma(vn[j], vn[j], ss);
+    ss = block_sum(ss, red);
+    double xnorm = sqrt(ss);
+    if (!(ss > 1e-290 && ss < 1e290)) {
+      double amax = 0.0;
+      for (int j = s + 2 + threadIdx.x; j < n; j += kT) amax = fmax(amax, fabs(vn[j]));
+      amax = block_max(amax, red);
+      xnorm = 0.0;
+      if (amax > 0.0) {
+        const double inv = 1.0 / amax;
+        double sq = 0.0;
+        for (int j = s + 2 + threadIdx.x; j < n; j += kT) {
+          const double q = vn[j] * inv;
+          sq += q * q;
+        }
+        xnorm = amax * sqrt(block_sum(sq, red));
+      }
+    }
+    if (threadIdx.x == 0) {
+      const double alpha = vn[s + 1];
+      if (xnorm == 0.0) {
+        sc[0] = 0.0;
+        sc[1] = alpha;
+        sc[2] = 0.0;
+      } else {
+        const double beta = -copysign(hypot(alpha, xnorm), alpha);
+        sc[0] = (beta - alpha) / beta;
+        sc[1] = beta;
+        sc[2] = 1.0 / (alpha - beta);
+      }
+    }
+    __syncthreads();
+    const double scal = sc[2];
+    for (int j = s + 2 + threadIdx.x; j < n; j += kT) vn[j] *= scal;
+    if (threadIdx.x == 0) vn[s + 1] = 1.0;
+    __syncthreads();
+    if (blockIdx.x == 0) {
+      for (int j = s + 1 + threadIdx.x; j < n; j += kT) Vh[(size_t)s * n + j] = vn[j];
+      if (threadIdx.x == 0) {
+        e[s] = sc[1];
+        tau[s] = sc[0];
+      }
+    }
+  };
+  // step 0: the reflector of row 0 as stored, then p = tau_0 A v_0
+  {
+    double* v0 = vbuf;
+    for (int j = 1 + threadIdx.x; j < n; j += kT) v0[j] = A[j];
+    if (blockIdx.x == 0 && threadIdx.x == 0) d[0] = A[0];
+    __syncthreads();
+    reflector(0, v0);
+    const double t0 = sc[0];
+    double mine = 0.0;
+    for (int i = first(1); i < n; i += W) {
+      const double* row = A + (size_t)i * n;
+      double s0 = 0.0;
+      for (int j = 1 + lane; j < n; j += 32) s0 += row[j] * v0[j];
+      const double pi = t0 * warp_sum(s0);
+      if (lane == 0) pbuf[i] = pi;
+      mine += pi * v0[i];
+    }
+    const double b = block_sum(lane == 0 ? mine : 0.0, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = b;
+  }
   grid.sync();
   for (int k = 0; k <= n - 3; ++k) {
-    const double* v = Vh + (size_t)k * n;
-    const double t = tau[k];
-    // p_i = t sum_j A[i][j] v[j] over the trailing block
-    double mine = 0.0;
-    for (int i = first(k + 1); i < n; i += W) {
-      const double* row = A + (size_t)i * n;
-      double s0 = 0.0, s1 = 0.0;
-      int j = k + 1 + lane;
-      for (; j + 32 < n; j += 64) {
-        s0 += row[j] * v[j];
-        s1 += row[j + 32] * v[j + 32];
-      }
-      if (j < n) s0 += row[j] * v[j];
-      const double s = warp_sum(s0 + s1);
-      const double pi = t * s;
-      if (lane == 0) p[i] = pi;
-      mine += pi * v[i];
-    }
-    if (lane == 0) sred[wib] = mine;
+    const double* v = vbuf + (size_t)(k & 1) * n;
+    double* vn = vbuf + (size_t)((k + 1) & 1) * n;
+    const double* p = pbuf + (size_t)(k & 1) * n;
+    double* pn = pbuf + (size_t)((k + 1) & 1) * n;
+    const double t = sc[0];  // tau_k of this block's reflector
+    double pv = 0.0;  // the block partials, summed by every warp in the same order
+    for (int b = lane; b < (int)gridDim.x; b += 32) pv += part[(k & 1) * gridDim.x + b];
+    pv = warp_sum(pv);
+    const double c = 0.5 * t * pv;
+    // row k+1 after step k's update, on the fly
+    const double v1 = v[k + 1], u1 = p[k + 1] - 2.0 * c * v1;
+    const double* row1 = A + (size_t)(k + 1) * n;
+    for (int j = k + 1 + threadIdx.x; j < n; j += kT)
+      vn[j] = row1[j] - fma(v1, p[j], u1 * v[j]);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double b = 0.0;
-      for (int q = 0; q < kT / 32; ++q) b += sred[q];
-      part[(k & 1) * gridDim.x + blockIdx.x] = b;
-    }
-    grid.sync();
-    if (threadIdx.x == 0) {
-      double pv = 0.0;
-      for (int b = 0; b < (int)gridDim.x; ++b) pv += part[(k & 1) * gridDim.x + b];
-      spv = pv;
-    }
-    __syncthreads();
-    const double c = 0.5 * t * spv;
-    // A22 -= v w^T + w v^T, w = p - c v; the owner of row k+1 then forms the
-    // next reflector from that row
-    for (int i = first(k + 1); i < n; i += W) {
-      double* row = A + (size_t)i * n;
-      const double vi = v[i], wi = p[i] - c * vi;
-      for (int j = k + 1 + lane; j < n; j += 32) {
-        const double vj = v[j], wj = p[j] - c * vj;
-        row[j] -= __dadd_rn(__dmul_rn(vi, wj), __dmul_rn(wi, vj));
-      }
-      if (i == k + 1 && k + 1 <= n - 3) {
-        __syncwarp();
-        house(A, n, k + 1, d, e, tau, Vh);
-      }
-    }
-    grid.sync();
-  }
-  if (gw == 0 && lane == 0) {
-    if (n >= 2) {
-      d[n - 2] = A[(size_t)(n - 2) * n + (n - 2)];
-      e[n - 2] = A[(size_t)(n - 2) * n + (n - 1)];
+    if (blockIdx.x == 0 && threadIdx.x == 0) d[k + 1] = vn[k + 1];
+    const bool last = k + 1 > n - 3;
+    double tn = 0.0;
+    if (!last) {
+      reflector(k + 1, vn);
+      tn = sc[0];
+    } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+      // n - 2: no reflector; the last subdiagonal (row n-2 is not written
+      // this step); the last diagonal comes from the owner of row n-1 below
+      e[n - 2] = vn[n - 1];
       tau[n - 2] = 0.0;
+      tau[n - 1] = 0.0;
     }
-    d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)];
-    tau[n - 1] = 0.0;
+    // step k's update of rows i >= k+2 (columns >= k+2) and step k+1's p
+    double mine = 0.0;
+    for (int i = first(k + 2); i < n; i += W) {
+      double* row = A + (size_t)i * n;
+      const double vi = v[i], ui = p[i] - 2.0 * c * vi;
+      double s0 = 0.0;
+      for (int j = k + 2 + lane; j < n; j += 32) {
+        const double a = row[j] - fma(vi, p[j], ui * v[j]);
+        row[j] = a;
+        s0 = fma(a, vn[j], s0);
+        if (last && i == n - 1 && j == n - 1) d[n - 1] = a;
+      }
+      if (!last) {
+        const double pi = tn * warp_sum(s0);
+        if (lane == 0) pn[i] = pi;
+        mine += pi * vn[i];
+      }
+    }
+    if (!last) {
+      const double b = block_sum(lane == 0 ? mine : 0.0, red);
+      if (threadIdx.x == 0) part[((k + 1) & 1) * gridDim.x + blockIdx.x] = b;
+    }
+    grid.sync();
   }
 }
 
@@ -339,7 +393,7 @@ __global__ void k_rotate(double* __restrict__ Q, int n, const int* __restrict__ 
 // secular roots: one warp per root.  Per merge m: kk = cnt[m] poles dn
 // (ascending) and weights zn at off[m]; rho = rho[m].  Root j lies in
 // (dn_j, dn_{j+1}) (the last in (dn_{kk-1}, dn_{kk-1} + rho sum z^2]); it is
-// found by bisection in tau = lambda - dn_o, o the nearer pole, with
+// found in tau = lambda - dn_o, o the nearer pole, on
 // f(tau) = 1 + rho sum_i z_i^2 / ((dn_i - dn_o) - tau).
 __global__ void k_secular(const double* __restrict__ dn, const double* __restrict__ zn,
                           const int* __restrict__ off, const int* __restrict__ cnt,
@@ -379,16 +433,37 @@ __global__ void k_secular(const double* __restrict__ dn, const double* __restric
     lo = 0.0;
     hi = r * warp_sum(s) * (1.0 + 8.0 * kEps);
   }
+  // safeguarded Newton on f (increasing in tau): the bracket [lo, hi] shrinks
+  // with the sign of f at every iterate; a Newton step that leaves it is
+  // replaced by bisection.  Ends when the step or the bracket is at the
+  // rounding level of tau (at most 200 evaluations).
+  double t = 0.5 * (lo + hi);
   for (int it = 0; it < 200; ++it) {
-    const double t = 0.5 * (lo + hi);
-    if (t == lo || t == hi) break;
-    if (hi - lo <= 2.0 * kEps * fmin(fabs(lo), fabs(hi))) break;
-    if (f_at(o, t) < 0.0) lo = t;
+    double s = 0.0, ds = 0.0;
+    for (int i = lane; i < kk; i += 32) {
+      const double q = 1.0 / ((d[i] - d[o]) - t);
+      const double zq = z[i] * q;
+      s += z[i] * zq;
+      ds += zq * zq;
+    }
+    s = warp_sum(s);
+    ds = warp_sum(ds);
+    const double f = 1.0 + r * s;
+    if (f == 0.0) break;
+    if (f < 0.0) lo = t;
     else hi = t;
+    if (!(hi - lo > 2.0 * kEps * fmax(fabs(lo), fabs(hi)))) break;
+    double tn = t - f / (r * ds);
+    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
+    if (fabs(tn - t) <= 2.0 * kEps * fabs(t)) {
+      t = tn;
+      break;
+    }
+    t = tn;
   }
   if (lane == 0) {
     orig[gr] = o;
-    tau[gr] = 0.5 * (lo + hi);
+    tau[gr] = t;
   }
 }
 
@@ -564,11 +639,45 @@ unsigned gblocks(long long work, int per = kT) {
     if (_e != cudaSuccess) return _e;                     \
   } while (0)
 
-template <typename T>
-cudaError_t put(T* dev, const std::vector<T>& h, cudaStream_t s) {
-  if (h.empty()) return cudaSuccess;
-  return cudaMemcpyAsync(dev, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s);
-}
+// Page-locked host memory for the merges' small transfers, so that each copy
+// is one asynchronous DMA instead of a staged pageable copy.  One buffer per
+// host thread, grown on demand: an upload region (filled sequentially and
+// rewound only after the stream has been synchronised, so that no queued copy
+// reads a rewritten byte) and a download region.
+struct Pinned {
+  char* p = nullptr;
+  size_t bytes = 0;
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost((void**)&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+};
+thread_local Pinned g_pinned;
+
+struct Stager {
+  char* base = nullptr;
+  size_t cap = 0, used = 0;
+  void rewind() { used = 0; }
+  template <typename T>
+  cudaError_t put(T* dev, const std::vector<T>& h, cudaStream_t s) {
+    if (h.empty()) return cudaSuccess;
+    const size_t b = sizeof(T) * h.size();
+    used = (used + 15) & ~(size_t)15;
+    if (used + b > cap) return cudaErrorMemoryAllocation;
+    std::memcpy(base + used, h.data(), b);
+    cudaError_t e = cudaMemcpyAsync(dev, base + used, b, cudaMemcpyHostToDevice, s);
+    used += b;
+    return e;
+  }
+};
 
 }  // namespace
 
@@ -598,8 +707,8 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
   double* d = C + nn;
   double* e = d + n;
   double* tau = e + n;
-  double* p = tau + n;
-  double* lam = p + n;
+  double* p = tau + n;        // 2 x n (by step parity)
+  double* lam = p + 2 * (size_t)n;
   double* z = lam + n;
   double* dn = z + n;
   double* zn = dn + n;
@@ -629,26 +738,45 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
   int* rot_idx = rot_off + n + 1;  // 2 per rotation
   int* leaf_lo = rot_idx + 2 * n;
   EK(cudaMemsetAsync(status, 0, sizeof(int), s));
+  // pinned host memory: uploads (at most ~40 n values between two
+  // synchronisations) then downloads (d, e, lam, z, tau: doubles; orig: ints)
+  const size_t up_bytes = (size_t)64 * 8 * (n + 64), down_doubles = (size_t)6 * n + 64;
+  EK(g_pinned.ensure(up_bytes + sizeof(double) * down_doubles));
+  Stager st;
+  st.base = g_pinned.p;
+  st.cap = up_bytes;
+  double* h_down = reinterpret_cast<double*>(g_pinned.p + up_bytes);
+  double* hd_p = h_down;            // n
+  double* he_p = hd_p + n;          // n
+  double* hz_p = he_p + n;          // n
+  double* htau_p = hz_p + n;        // n
+  int* horig_p = reinterpret_cast<int*>(htau_p + n);  // n ints
+  double* hlam_p = htau_p + 2 * n;  // n
 
   // ---- 1. tridiagonalisation
   if (n >= 3) {
     int dev = 0, nsm = 0, per_sm = 0;
     EK(cudaGetDevice(&dev));
     EK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    EK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, kT, 0));
+    const size_t smem = sizeof(double) * (2 * (size_t)n + kT / 32);
+    EK(cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    EK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, kT, smem));
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
     // one block per SM (the rows of a step spread over every SM's FP64
     // pipe), fewer when there are fewer rows than warps
-    int grid = std::max(1, std::min((n + kT / 32 - 1) / (kT / 32), nsm * std::max(per_sm, 1)));
+    int grid = std::max(1, std::min(n / 2, nsm * per_sm));
     grid = std::min(grid, nsm);
     void* args[] = {&A, &n, &d, &e, &tau, &Vh, &p, &part};
-    EK(cudaLaunchCooperativeKernel((void*)k_sytrd, dim3(grid), dim3(kT), args, 0, s));
+    EK(cudaLaunchCooperativeKernel((void*)k_sytrd, dim3(grid), dim3(kT), args, smem, s));
   }
   EK(mark(1));
   std::vector<double> hd(n), he(n > 1 ? n - 1 : 1, 0.0);
   if (n >= 3) {
-    EK(cudaMemcpyAsync(hd.data(), d, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-    EK(cudaMemcpyAsync(he.data(), e, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, s));
+    EK(cudaMemcpyAsync(hd_p, d, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    EK(cudaMemcpyAsync(he_p, e, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, s));
     EK(cudaStreamSynchronize(s));
+    std::memcpy(hd.data(), hd_p, sizeof(double) * n);
+    std::memcpy(he.data(), he_p, sizeof(double) * (n - 1));
   } else {
     std::vector<double> ha(nn);
     EK(cudaMemcpyAsync(ha.data(), A, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
@@ -677,16 +805,18 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
     const int nleaf = 1 << L;
     std::vector<int> llo(nleaf + 1);
     for (int c = 0; c <= nleaf; ++c) llo[c] = (int)(((long long)c * n) >> L);
-    EK(put(leaf_lo, llo, s));
-    EK(cudaMemcpyAsync(dn, dmod.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    EK(cudaMemcpyAsync(zn, he.data(), sizeof(double) * he.size(), cudaMemcpyHostToDevice, s));
+    EK(st.put(leaf_lo, llo, s));
+    EK(st.put(dn, dmod, s));
+    EK(st.put(zn, he, s));
     EK(cudaMemsetAsync(Q, 0, sizeof(double) * nn, s));
     k_leaf_ql<<<nleaf, 32, 0, s>>>(dn, zn, leaf_lo, nleaf, n, lam, Q, status);
     EK(cudaGetLastError());
   }
   std::vector<double> hlam(n);
-  EK(cudaMemcpyAsync(hlam.data(), lam, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  EK(cudaMemcpyAsync(hlam_p, lam, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
   EK(cudaStreamSynchronize(s));
+  st.rewind();
+  std::memcpy(hlam.data(), hlam_p, sizeof(double) * n);
   for (int lev = L - 1; lev >= 0; --lev) {
     const int nm = 1 << lev;
     std::vector<int> hlo, hmid, hhi;
@@ -704,17 +834,18 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
     }
     const int nmerge = (int)hlo.size();
     if (nmerge == 0) continue;
-    EK(put(mlo, hlo, s));
-    EK(put(mmid, hmid, s));
-    EK(put(mhi, hhi, s));
-    EK(put(sgn, hs, s));
+    EK(st.put(mlo, hlo, s));
+    EK(st.put(mmid, hmid, s));
+    EK(st.put(mhi, hhi, s));
+    EK(st.put(sgn, hs, s));
     int maxk = 0;
     for (int q = 0; q < nmerge; ++q) maxk = std::max(maxk, hhi[q] - hlo[q]);
     k_merge_z<<<dim3(gblocks(maxk), nmerge), kT, 0, s>>>(Q, n, mlo, mmid, mhi, sgn, nmerge, z);
     EK(cudaGetLastError());
-    std::vector<double> hz(n);
-    EK(cudaMemcpyAsync(hz.data(), z, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    EK(cudaMemcpyAsync(hz_p, z, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     EK(cudaStreamSynchronize(s));
+    st.rewind();
+    const double* hz = hz_p;
     // deflation on the host, per merge
     std::vector<int> hoff(nmerge + 1, 0), hcnt(nmerge), hcolN, hdcoff(nmerge + 1, 0), hdcol,
         hroff(nmerge + 1, 0), hridx, hgoff(nmerge), hsoff(nmerge), hroot_merge;
@@ -788,20 +919,20 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
       for (int t = 0; t < hcnt[q]; ++t) hroot_merge.push_back(q);
     }
     const int nroots = (int)hdn.size();
-    EK(put(off, hoff, s));
-    EK(put(cnt, hcnt, s));
-    EK(put(colN, hcolN, s));
-    EK(put(dcol_off, hdcoff, s));
-    EK(put(dcol, hdcol, s));
-    EK(put(rot_off, hroff, s));
-    EK(put(rot_idx, hridx, s));
-    EK(put(rot_cs, hrcs, s));
-    EK(put(goff, hgoff, s));
-    EK(put(soff, hsoff, s));
-    EK(put(root_merge, hroot_merge, s));
-    EK(put(dn, hdn, s));
-    EK(put(zn, hzn, s));
-    EK(put(rho, hr, s));
+    EK(st.put(off, hoff, s));
+    EK(st.put(cnt, hcnt, s));
+    EK(st.put(colN, hcolN, s));
+    EK(st.put(dcol_off, hdcoff, s));
+    EK(st.put(dcol, hdcol, s));
+    EK(st.put(rot_off, hroff, s));
+    EK(st.put(rot_idx, hridx, s));
+    EK(st.put(rot_cs, hrcs, s));
+    EK(st.put(goff, hgoff, s));
+    EK(st.put(soff, hsoff, s));
+    EK(st.put(root_merge, hroot_merge, s));
+    EK(st.put(dn, hdn, s));
+    EK(st.put(zn, hzn, s));
+    EK(st.put(rho, hr, s));
     int maxkk = 0;
     for (int q = 0; q < nmerge; ++q) maxkk = std::max(maxkk, hcnt[q]);
     if (!hridx.empty()) {
@@ -827,12 +958,13 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
     }
     // the merged eigenvalues: roots (lambda_j = dn_{o_j} + tau_j) and the
     // deflated values, sorted per merge; the new column order
-    std::vector<int> horig(nroots);
-    std::vector<double> htau(nroots);
+    const int* horig = horig_p;
+    const double* htau = htau_p;
     if (nroots > 0) {
-      EK(cudaMemcpyAsync(horig.data(), orig, sizeof(int) * nroots, cudaMemcpyDeviceToHost, s));
-      EK(cudaMemcpyAsync(htau.data(), tauv, sizeof(double) * nroots, cudaMemcpyDeviceToHost, s));
+      EK(cudaMemcpyAsync(horig_p, orig, sizeof(int) * nroots, cudaMemcpyDeviceToHost, s));
+      EK(cudaMemcpyAsync(htau_p, tauv, sizeof(double) * nroots, cudaMemcpyDeviceToHost, s));
       EK(cudaStreamSynchronize(s));
+      st.rewind();
     }
     std::vector<int> hdst, hdstoff(nmerge + 1, 0);
     for (int q = 0; q < nmerge; ++q) {
@@ -854,8 +986,8 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
       }
       hdstoff[q + 1] = (int)hdst.size();
     }
-    EK(put(dst_off, hdstoff, s));
-    EK(put(dst, hdst, s));
+    EK(st.put(dst_off, hdstoff, s));
+    EK(st.put(dst, hdst, s));
     k_copy_deflated<<<dim3(gblocks((long long)maxk * maxk), nmerge), kT, 0, s>>>(
         Q, n, mlo, mhi, cnt, dcol_off, dcol, nmerge, X);
     EK(cudaGetLastError());
@@ -863,7 +995,7 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
         Q, n, mlo, mhi, cnt, goff, dst_off, dst, C, X, nmerge);
     EK(cudaGetLastError());
   }
-  EK(cudaMemcpyAsync(w, hlam.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  EK(st.put(w, hlam, s));
 
   // ---- 3. back-transformation into A
   EK(mark(2));
