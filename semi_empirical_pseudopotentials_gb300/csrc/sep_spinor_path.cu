@@ -16,6 +16,10 @@
 //   ortho          filter/ortho.c's two-level Gram scheme on the Hermitian
 //                  Gram matrix (in place of zgesvd, ortho.c:5-40);
 //   Rayleigh-Ritz  projected H, Hermitian eigensolve, rotation (Hmat.c:5-75);
+//                  the Hermitian eigensolves run on the library's symmetric
+//                  solver (sep_eigh.cu) through the real embedding
+//                  [[Re H, -Im H], [Im H, Re H]] (cuSOLVER's Zheevd with
+//                  sep_ctx_set_eigensolver(ctx, 0));
 //   sigma          |H psi - E psi| (energy.c:114-145 forms the same
 //                  quantity as sqrt(<H^2> - <H>^2)).
 // Complex products run on the real subspace contractions: for rows x = a+ib
@@ -34,6 +38,7 @@
 #include "../../include/sep_gb300.h"
 #include "sep_ctx.cuh"
 #include "sep_ctx_detail.cuh"
+#include "sep_eigh.cuh"
 
 namespace sep {
 
@@ -177,8 +182,139 @@ int spinor_h(sep_ctx* c, const double* psi, double* out, long long nsp) {
   return kOk;
 }
 
-// complex Hermitian eigensolve (column-major, in place), w ascending
+// M (2m x 2m, symmetric) = [[Re H, -Im H], [Im H, Re H]] for the Hermitian H
+// whose upper triangle A holds (column-major): H_ij = A[i + j m] for i <= j,
+// conj(A[j + i m]) otherwise
+__global__ void k_embed(const cuDoubleComplex* __restrict__ A, long long m,
+                        double* __restrict__ M) {
+  const long long n2 = 2 * m;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n2 * n2;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long r = t / n2, q = t - r * n2;
+    const long long i = r % m, j = q % m, bi = r / m, bj = q / m;
+    cuDoubleComplex h = (i <= j) ? A[i + j * m] : cuConj(A[j + i * m]);
+    M[t] = (bi == bj) ? h.x : (bi == 1 ? h.y : -h.y);
+  }
+}
+
+// The complex eigenvectors from those of the real embedding: an eigenpair
+// (lambda, u + i v) of H gives M the two eigenvectors [u; v] and [-v; u], so
+// the real spectrum holds each lambda twice.  Per cluster of equal real
+// eigenvalues (2 q of them: q complex eigenvectors), the complex candidates
+// u + i v of all 2 q real vectors span the complex eigenspace; q of them are
+// chosen by Gram-Schmidt with pivoting on the largest remaining norm, so a
+// pair (c, i c) is never taken twice.  vr: the real eigenvectors
+// (column-major, 2m x 2m), wr: their eigenvalues ascending; out: column-major
+// complex m x m and w (m).  Host arithmetic, O(m^2) per cluster member.
+int embed_to_complex(long long m, const std::vector<double>& wr, const std::vector<double>& vr,
+                     std::vector<cuDoubleComplex>& out, std::vector<double>& w) {
+  const long long n2 = 2 * m;
+  double scale = 1.0;
+  for (double x : wr) scale = std::max(scale, std::fabs(x));
+  const double tol = 1e-10 * scale;
+  out.assign((size_t)(m * m), make_cuDoubleComplex(0.0, 0.0));
+  w.assign((size_t)m, 0.0);
+  long long oc = 0;
+  long long i = 0;
+  std::vector<std::vector<double>> re, im;
+  while (i < n2) {
+    long long j = i + 1;
+    while (j < n2 && std::fabs(wr[(size_t)j] - wr[(size_t)j - 1]) <= tol) ++j;
+    const long long size = j - i, want = size / 2;
+    re.assign((size_t)size, std::vector<double>((size_t)m));
+    im.assign((size_t)size, std::vector<double>((size_t)m));
+    for (long long t = 0; t < size; ++t)
+      for (long long r = 0; r < m; ++r) {
+        re[(size_t)t][(size_t)r] = vr[(size_t)((i + t) * n2 + r)];
+        im[(size_t)t][(size_t)r] = vr[(size_t)((i + t) * n2 + m + r)];
+      }
+    std::vector<bool> used((size_t)size, false);
+    for (long long s = 0; s < want; ++s) {
+      long long best = -1;
+      double bn = -1.0;
+      for (long long t = 0; t < size; ++t) {
+        if (used[(size_t)t]) continue;
+        double nn = 0.0;
+        for (long long r = 0; r < m; ++r)
+          nn += re[(size_t)t][(size_t)r] * re[(size_t)t][(size_t)r] +
+                im[(size_t)t][(size_t)r] * im[(size_t)t][(size_t)r];
+        if (nn > bn) {
+          bn = nn;
+          best = t;
+        }
+      }
+      if (best < 0 || !(bn > 1e-12) || oc >= m) {
+        set_error("spinor path: the real embedding's eigenvectors do not pair up");
+        return kErrNumeric;
+      }
+      used[(size_t)best] = true;
+      const double inv = 1.0 / std::sqrt(bn);
+      std::vector<double>& qr = re[(size_t)best];
+      std::vector<double>& qi = im[(size_t)best];
+      for (long long r = 0; r < m; ++r) {
+        qr[(size_t)r] *= inv;
+        qi[(size_t)r] *= inv;
+        out[(size_t)(r + oc * m)] = make_cuDoubleComplex(qr[(size_t)r], qi[(size_t)r]);
+      }
+      w[(size_t)oc] = wr[(size_t)(i + 2 * s)];
+      ++oc;
+      // remove q from the others: x -= q <q|x>
+      for (long long t = 0; t < size; ++t) {
+        if (used[(size_t)t]) continue;
+        double pr = 0.0, pi = 0.0;
+        for (long long r = 0; r < m; ++r) {
+          const double xr = re[(size_t)t][(size_t)r], xi = im[(size_t)t][(size_t)r];
+          pr += qr[(size_t)r] * xr + qi[(size_t)r] * xi;
+          pi += qr[(size_t)r] * xi - qi[(size_t)r] * xr;
+        }
+        for (long long r = 0; r < m; ++r) {
+          re[(size_t)t][(size_t)r] -= pr * qr[(size_t)r] - pi * qi[(size_t)r];
+          im[(size_t)t][(size_t)r] -= pr * qi[(size_t)r] + pi * qr[(size_t)r];
+        }
+      }
+    }
+    i = j;
+  }
+  if (oc != m) {
+    set_error("spinor path: the real embedding's eigenvalues do not come in pairs");
+    return kErrNumeric;
+  }
+  return kOk;
+}
+
+// complex Hermitian eigensolve (column-major, in place, upper triangle read),
+// w ascending.  c->eigensolver 1: the library's solver on the real embedding;
+// 0: cuSOLVER's Zheevd.
 int heevd(sep_ctx* c, cuDoubleComplex* A, long long m, double* w) {
+  if (c->eigensolver == 1) {
+    const long long n2 = 2 * m;
+    const size_t wd = eigh::work_doubles(n2);
+    RET(grow(c, c->w_eigh, sizeof(double) * (wd + (size_t)(n2 * n2) + (size_t)n2)));
+    double* work = c->w_eigh.as<double>();
+    double* M = work + wd;
+    double* wr = M + n2 * n2;
+    k_embed<<<blocks(n2 * n2), kT, 0, c->stream>>>(A, m, M);
+    CK(cudaGetLastError());
+    int bad = 0;
+    CK(eigh::solve(M, (int)n2, wr, work, c->stream, &bad));
+    if (bad) {
+      set_error("spinor path: the QL iteration of a leaf did not converge");
+      return kErrSolver;
+    }
+    std::vector<double> hw((size_t)n2), hv((size_t)(n2 * n2));
+    CK(cudaMemcpyAsync(hw.data(), wr, sizeof(double) * n2, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hv.data(), M, sizeof(double) * n2 * n2, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<cuDoubleComplex> hc;
+    std::vector<double> hwc;
+    RET(embed_to_complex(m, hw, hv, hc, hwc));
+    CK(cudaMemcpyAsync(A, hc.data(), sizeof(cuDoubleComplex) * m * m, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemcpyAsync(w, hwc.data(), sizeof(double) * m, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return kOk;
+  }
   int lwork = 0;
   if (cusolverDnZheevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER,
                                   (int)m, A, (int)m, w, &lwork) != CUSOLVER_STATUS_SUCCESS) {

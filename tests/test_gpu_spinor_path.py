@@ -126,3 +126,23 @@ def test_spinor_filter_against_oracle_on_a_larger_case():
     for s in range(3):
         ref = so.newton_filter(start[s], an, zn, dE_1, vmin, pot, ks, dims, nlc, nl, h, h ** 3)
         assert np.abs(got[s] - ref).max() <= 1e-11 * np.abs(ref).max(), s
+
+
+def test_spinor_pipeline_library_eigensolver_matches_cusolver():
+    """The whole spinor program on the 32^3 case with the library's solver
+    (on the real embedding of each Hermitian problem) and with cuSOLVER's
+    Zheevd: the same kept count, Ritz values to 1e-10 and sigma to 1e-8."""
+    dims, h, nlc, nl, pot = larger_case()
+    out = {}
+    for mode in (1, 0):
+        ctx = binding.Context(dims, (h, h, h), potl=pot, ekinmax=EKINMAX)
+        ctx.set_eigensolver(mode)
+        sp = spinor.SpinorPath(ctx, nlc, nl, sigma=h)
+        n = ctx.ngrid
+        st = O.start_states(-4242, 8, n, ctx.dv)
+        spinors = np.stack([np.concatenate([st[2 * j], st[2 * j + 1]]) for j in range(4)])
+        out[mode] = sp.pipeline(spinors.astype(np.complex128), [-0.8, -0.6, -0.4], 64)
+        ctx.close()
+    assert out[0]["mkept"] == out[1]["mkept"]
+    assert np.abs(out[0]["eval"] - out[1]["eval"]).max() <= 1e-10
+    assert np.abs(out[0]["sigma"] - out[1]["sigma"]).max() <= 1e-8
