@@ -280,7 +280,7 @@ TRAFFIC_PER_PAIR_128 = {"y_fwd": (201.354752e6 + 142.915584e6) / 12,
                         "y_inv": (201.346304e6 + 143.166208e6) / 12,
                         "x_inv_epi_fwd": (444.561152e6 + 351.911936e6) / 12,
                         # profiles/xy_plane_pass_c64_128.md (6 pairs)
-                        "xy_inv_epi_fwd": (214.69952e6 + 147.428864e6) / 6}
+                        "xy_inv_epi_fwd": (209.92256e6 + 147.293952e6) / 6}
 
 
 def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):

@@ -2,24 +2,34 @@
 // (see sep_ozaki.cuh for the arithmetic).
 //
 // Kernel shape (k_oz_mma): one CTA per SM, persistent over work items (an
-// output tile of 128 x 64 and a range of K), nine warps with fixed roles:
-//  * warp 17, one thread: the bulk copies (cp.async.bulk, mbarrier
-//    transaction counts) of the pre-tiled slice blocks, kStages stages ahead.
-//  * warp 16, one thread: the tcgen05.mma instructions.
-//  * warps 0-7 and 8-15: the drains of the tile's two 32-column halves
-//    ("sets").  The kSlices level accumulators of a set live in TMEM (kSlices
-//    x 32 FP32 columns of 128 lanes; set c at columns 256 c).  Every kDrainK
-//    of K a set's eight warps read them back with tcgen05.ld (warp w: lanes
-//    32 (w % 4) .. + 31, 16 of the set's columns) and add them into two int64
+// output tile of 128 x 64 and a range of K), 19 warps with fixed roles:
+//  * warp 18, one thread: the copies of each stage, kStages stages ahead: A's
+//    pre-tiled slice block in one bulk copy (cp.async.bulk), and for each of
+//    the tile's two 32-column halves of B ("sets") the 1 KB pieces of all
+//    digits in one 3-D tensor copy (cp.async.bulk.tensor), with mbarrier
+//    transaction counts.
+//  * warps 16 and 17, one thread each: the tcgen05.mma instructions of set 0
+//    and set 1.  Each walks the stages in order with precomputed descriptors;
+//    the stage buffer is released when both sets have committed to it.  A
+//    single thread issuing both sets kept the tensor pipe about half as busy:
+//    its scheduling work ran serially with the MMA issue.
+//  * warps 0-7 and 8-15: the drains of set 0 and set 1.  The kSlices level
+//    accumulators of a set live in TMEM (kSlices x 32 FP32 columns of 128
+//    lanes; set c at columns 256 c).  Every kDrainK of K a set's eight warps
+//    read them back with tcgen05.ld (warp w: lanes 32 (w % 4) .. + 31, 16 of
+//    the set's columns, two levels per wait) and add them into two int64
 //    fixed-point registers per output element: levels 0-3 in units of 2^-24
 //    of level 0, levels 4-6 in units of 2^-48.
-// The two sets drain kDrainK / 2 of K apart; while one set is drained the MMA
-// thread keeps issuing the other set's products, up to kStages stages ahead,
-// so the tensor cores do not wait for the drains.
+// The two sets drain kDrainK / 2 of K apart; while one set is drained the
+// other set's thread keeps issuing, up to kStages - 1 stages ahead, so the
+// tensor cores do not wait for the drains.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "sep_ozaki.cuh"
 
@@ -31,8 +41,8 @@ constexpr int kSets = 2;                                   // 32-column halves o
 constexpr int kSetN = kTileN / kSets;                      // 32
 constexpr int kDrainWarps = 8 * kSets;                     // warps 0..15
 constexpr int kDrainCols = kSetN / 2;                      // columns per drain thread
-constexpr int kMmaWarp = kDrainWarps, kLoadWarp = kDrainWarps + 1;
-constexpr int kThreads = 32 * (kDrainWarps + 2);           // + the MMA and copy warps
+constexpr int kMmaWarp = kDrainWarps, kLoadWarp = kDrainWarps + kSets;  // a MMA warp per set
+constexpr int kThreads = 32 * (kDrainWarps + kSets + 1);   // + the MMA and copy warps
 constexpr int kStages = 4;
 constexpr int kStageA = kSlices * kTileM * kChunkK * 2;    // 28672 bytes: one block
 constexpr int kStageB = kSlices * kTileN * kChunkK * 2;    // 14336 bytes: 64 rows
@@ -44,6 +54,7 @@ constexpr int kTmemCols = 512;                              // set c: 256 c .. +
 constexpr int kSetCols = 256;
 constexpr int kStagesPerDrain = kDrainK / kChunkK;          // 8
 constexpr long long kSpin = 1LL << 26;                      // bounded waits
+constexpr int kL2Ahead = 8;  // stages between an operand block's L2 prefetch and its copy
 static_assert(kSlices * kSetN <= kSetCols && kSets * kSetCols <= kTmemCols, "TMEM columns");
 static_assert((kSlices * kSetN) % 16 == 0, "one MMA per digit of A and set");
 static_assert((kSlices) * kDrainK * 16384LL < (1LL << 24), "exact FP32 level sums");
@@ -90,6 +101,21 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
           dst),
       "l"(src), "r"(bytes), "r"(bar)
       : "memory");
+}
+
+// 3-D tensor copy (B operand: the 7 digit pieces of one set, 1 KB each, 4 KB
+// apart in global memory, consecutive in shared memory)
+__device__ __forceinline__ void tensor3_g2s(uint32_t dst, const CUtensorMap* map, int c0, int c1,
+                                            int c2, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -144,6 +170,24 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
       : "r"(taddr)
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// two loads of 16 columns (levels at a0 and a1) with one wait: the second
+// load's latency runs under the first's
+__device__ __forceinline__ void tmem_ld16x2(uint32_t a0, uint32_t a1, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%32];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%33];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(a0), "r"(a1)
+      : "memory");
 }
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
@@ -350,7 +394,7 @@ __device__ __forceinline__ void item_of(const MmaArgs& a, int item, int& split, 
   nst = (int)(kc1 > kc0 ? kc1 - kc0 : 0);  // the host leaves no split empty
 }
 
-__global__ void __maxnreg__(96) k_oz_mma(const MmaArgs a) {
+__global__ void __maxnreg__(96) k_oz_mma(const MmaArgs a, const __grid_constant__ CUtensorMap tmb) {
   extern __shared__ __align__(1024) uint8_t stage_mem[];
   __shared__ __align__(8) uint64_t bar_load[kStages];   // copies of a stage landed
   __shared__ __align__(8) uint64_t bar_free[kStages];   // both sets' products of a stage done
@@ -394,118 +438,98 @@ __global__ void __maxnreg__(96) k_oz_mma(const MmaArgs a) {
         long long kc0;
         item_of(a, item, split, tm, tn, kc0, nst);
         const uint16_t* ablk = a.A + (long long)tm * a.nkc * kBlockElems;
-        const uint16_t* bblk = a.B + (long long)(tn >> 1) * a.nkc * kBlockElems +
-                               (tn & 1) * kSets * (kSetSliceBytes / 2);
+        const uint16_t* bblk = a.B + (long long)(tn >> 1) * a.nkc * kBlockElems;
+        // B pieces: 1 KB piece (tn & 1) * kSets + c of every digit of block
+        // ((tn >> 1) nkc + kc), the tensor's third coordinate counting digits
+        const int piece0 = (tn & 1) * kSets;
+        const long long dig0 = (long long)(tn >> 1) * a.nkc * kSlices;
         for (int st = 0; st < nst && ok; ++st, ++gs) {
           const int b = (int)(gs % kStages);
+          const long long kc = kc0 + st;
+          if (kL2Ahead > 0 && st + kL2Ahead < nst) {  // warm L2 for a later stage
+            prefetch_l2(ablk + (kc + kL2Ahead) * kBlockElems, (uint32_t)(kBlockElems * 2));
+            prefetch_l2(bblk + (kc + kL2Ahead) * kBlockElems, (uint32_t)(kBlockElems * 2));
+          }
           // the buffer's previous stage: both sets' products done
           if (gs >= kStages)
             ok = mbar_wait(smem_u32(&bar_free[b]), (uint32_t)((gs / kStages - 1) & 1), a.err, 2);
           if (!ok) break;
           const uint32_t base = smem0 + b * kStageBytes, bar = smem_u32(&bar_load[b]);
-          const long long kc = kc0 + st;
           mbar_expect_tx(bar, kStageBytes);
           bulk_g2s(base, ablk + kc * kBlockElems, kStageA, bar);
           // set c's 32 rows of every digit, digits consecutive: any run of
           // digits of one set is one operand of 32 rows per digit
-#pragma unroll 1
+#pragma unroll
           for (int c = 0; c < kSets; ++c)
-#pragma unroll 1
-            for (int t = 0; t < kSlices; ++t)
-              bulk_g2s(base + kStageA + (c * kSlices + t) * kSetSliceBytes,
-                       bblk + kc * kBlockElems + t * (kSliceBytes / 2) + c * (kSetSliceBytes / 2),
-                       kSetSliceBytes, bar);
+            tensor3_g2s(base + kStageA + c * kSlices * kSetSliceBytes, &tmb, 0, piece0 + c,
+                        (int)(dig0 + kc * kSlices), bar);
         }
       }
       // the last copies of every buffer land before the shared memory is released
       for (long long g = (gs > kStages ? gs - kStages : 0); g < gs; ++g)
         mbar_wait(smem_u32(&bar_load[g % kStages]), (uint32_t)((g / kStages) & 1), a.err, 4);
     }
-  } else if (warp == kMmaWarp) {
-    // ---------------- products ----------------
-    if ((tid & 31) == 0) {
-      long long g0 = 0;         // global stage index of the item's first stage
-      long long seen = -1;      // last global stage whose copies were seen landed
-      uint32_t f0 = 0, f1 = 0;  // periods ended (bar_full commits) per set
-      uint32_t d0 = 0, d1 = 0;  // drains seen complete per set
+  } else if (warp == kMmaWarp || warp == kMmaWarp + 1) {
+    // ---------------- products: one thread per set ----------------
+    // Each set's thread walks the stages in order: it waits for the stage's
+    // copies, issues the set's kSlices MMAs and commits them to the stage
+    // buffer's barrier (which the copy thread waits on, for both sets,
+    // before it reuses the buffer, so a set runs at most kStages - 1 stages
+    // ahead of the other).  Before the first stage of a period it waits for
+    // the set's accumulators to be drained.
+    auto products = [&](auto cc) {
+      constexpr int c = decltype(cc)::value;
+      // descriptors of stage buffer 0 (digit 0 of A, set c of B); a buffer
+      // and a digit are fixed byte offsets added to the start-address field
+      // (shared addresses < 2^18, so the 14-bit field never carries)
+      const uint64_t da0 = smem_desc(smem0, 128, kRowGroupStride);
+      const uint64_t db0 = smem_desc(smem0 + kStageA + c * kSlices * kSetSliceBytes, 128, kRowGroupStride);
+      const uint32_t dt = tmem + (uint32_t)(c * kSetCols);
+      long long g0 = 0;        // global stage index of the item's first stage
+      uint32_t nf = 0, nd = 0;  // periods ended (bar_full commits), drains seen complete
       for (int item = blockIdx.x; item < items && ok; item += gridDim.x) {
         int split, tm, tn, nst;
         long long kc0;
         item_of(a, item, split, tm, tn, kc0, nst);
-        int n0 = 0, n1 = 0;  // next local stage per set
-        while (ok && (n0 < nst || n1 < nst)) {
-          // a set may run at most kStages - 1 stages ahead of the other: the
-          // copies of a stage wait for the buffer's previous stage
-          const int lo = min(n0, n1);
-          // the set that is behind first; a set whose new period needs its
-          // accumulators drained waits, and the other set goes on
-          bool done_one = false;
-          for (int pass = 0; pass < 2 && ok && !done_one; ++pass) {
-            const int c = ((n0 <= n1) ? 0 : 1) ^ pass;
-            int& nx = c ? n1 : n0;
-            uint32_t& nf = c ? f1 : f0;
-            uint32_t& nd = c ? d1 : d0;
-            const int st = nx;
-            if (st >= nst || st >= lo + kStages) continue;
-            const bool fresh = st == 0 || drain_after(c, st - 1, nst);
-            if (fresh && nd < nf) {
-              if (!mbar_try(smem_u32(&bar_drained[c]), nd & 1)) continue;
-              ++nd;
-              if (nd < nf) continue;
-            }
-            const long long gs = g0 + st;
-            const int b = (int)(gs % kStages);
-            if (gs > seen) {  // the first set to reach a stage waits for its copies
-              ok = mbar_wait(smem_u32(&bar_load[b]), (uint32_t)((gs / kStages) & 1), a.err, 1);
-              if (!ok) break;
-              seen = gs;
-            }
-            tc_fence_after();
-            const uint32_t base = smem0 + b * kStageBytes;
-            const uint64_t db =
-                smem_desc(base + kStageA + c * kSlices * kSetSliceBytes, 128, kRowGroupStride);
-            // digit s of A times digits 0 .. kSlices-1-s of B: the
-            // accumulators of levels s .. kSlices-1, adjacent in TMEM
-#pragma unroll 1
-            for (int s = 0; s < kSlices; ++s) {
-              const uint64_t da = smem_desc(base + s * kSliceBytes, 128, kRowGroupStride);
-              mma_bf16(tmem + (uint32_t)(c * kSetCols + s * kSetN), da, db,
-                       idesc_bf16(kTileM, (kSlices - s) * kSetN), (fresh && s == 0) ? 0u : 1u);
-            }
-            mma_commit(smem_u32(&bar_free[b]));
-            if (drain_after(c, st, nst)) {
-              mma_commit(smem_u32(&bar_full[c]));
-              ++nf;
-            }
-            ++nx;
-            done_one = true;
+        for (int st = 0; st < nst; ++st) {
+          const bool fresh = st == 0 || drain_after(c, st - 1, nst);
+          if (fresh && nd < nf) {
+            ok = mbar_wait(smem_u32(&bar_drained[c]), nd & 1, a.err, 3);
+            if (!ok) break;
+            ++nd;
           }
-          if (ok && !done_one) {
-            // both sets wait for a drain: block on the set that is behind
-            int c = (n0 <= n1) ? 0 : 1;
-            if ((c ? n1 : n0) >= nst) c ^= 1;
-            uint32_t& nf = c ? f1 : f0;
-            uint32_t& nd = c ? d1 : d0;
-            if (nd < nf) {
-              ok = mbar_wait(smem_u32(&bar_drained[c]), nd & 1, a.err, 3);
-              if (ok) ++nd;
-            } else {  // nothing to wait for and nothing issued: a logic error
-              atomicCAS(a.err, 0, 7);
-              ok = false;
-            }
+          const unsigned long long gs = (unsigned long long)(g0 + st);
+          const uint32_t b = (uint32_t)(gs % kStages);
+          ok = mbar_wait(smem_u32(&bar_load[b]), (uint32_t)((gs / kStages) & 1), a.err, 1);
+          if (!ok) break;
+          tc_fence_after();
+          const uint64_t so = (uint64_t)((b * (uint32_t)kStageBytes) >> 4);
+          // digit s of A times digits 0 .. kSlices-1-s of B: the accumulators
+          // of levels s .. kSlices-1, adjacent in TMEM
+#pragma unroll
+          for (int s = 0; s < kSlices; ++s)
+            mma_bf16(dt + (uint32_t)(s * kSetN), da0 + so + (uint64_t)((s * kSliceBytes) >> 4),
+                     db0 + so, idesc_bf16(kTileM, (kSlices - s) * kSetN),
+                     (fresh && s == 0) ? 0u : 1u);
+          mma_commit(smem_u32(&bar_free[b]));
+          if (drain_after(c, st, nst)) {
+            mma_commit(smem_u32(&bar_full[c]));
+            ++nf;
           }
         }
         g0 += nst;
       }
-      // the last drains of both sets before the accumulators are released
-      while (ok && d0 < f0) {
-        ok = mbar_wait(smem_u32(&bar_drained[0]), d0 & 1, a.err, 5);
-        if (ok) ++d0;
+      // the last drain before the accumulators are released
+      while (ok && nd < nf) {
+        ok = mbar_wait(smem_u32(&bar_drained[c]), nd & 1, a.err, 5);
+        if (ok) ++nd;
       }
-      while (ok && d1 < f1) {
-        ok = mbar_wait(smem_u32(&bar_drained[1]), d1 & 1, a.err, 5);
-        if (ok) ++d1;
-      }
+    };
+    if ((tid & 31) == 0) {
+      if (warp == kMmaWarp)
+        products(std::integral_constant<int, 0>{});
+      else
+        products(std::integral_constant<int, 1>{});
     }
   } else {
     // ---- drains: set c = warp / 8, lanes 32 (warp % 4) .. + 31, columns
@@ -526,17 +550,31 @@ __global__ void __maxnreg__(96) k_oz_mma(const MmaArgs a) {
         if (!ok) break;
         ++nfull_seen;
         tc_fence_after();
+        const uint32_t t0 = tmem + lane_base + (uint32_t)(c * kSetCols + h * kDrainCols);
+        // levels in pairs, two loads in flight per wait
 #pragma unroll
-        for (int l = 0; l < kSlices; ++l) {
-          uint32_t v[kDrainCols];
-          tmem_ld16(tmem + lane_base + (uint32_t)(c * kSetCols + l * kSetN + h * kDrainCols), v);
+        for (int l0 = 0; l0 < kSlices; l0 += 2) {
+          uint32_t v[2 * kDrainCols];
+          if (l0 + 1 < kSlices) {
+            tmem_ld16x2(t0 + (uint32_t)(l0 * kSetN), t0 + (uint32_t)((l0 + 1) * kSetN), v);
+          } else {
+            uint32_t (&v0)[kDrainCols] = *reinterpret_cast<uint32_t(*)[kDrainCols]>(v);
+            tmem_ld16(t0 + (uint32_t)(l0 * kSetN), v0);
+          }
 #pragma unroll
-          for (int j = 0; j < kDrainCols; ++j) {
-            const long long w = (long long)__float2int_rn(__uint_as_float(v[j]));
-            if (l <= 3)
-              Rh[j] += w << (24 - 8 * l);
-            else
-              Rl[j] += w << (48 - 8 * l);
+          for (int q = 0; q < 2; ++q) {
+            const int l = l0 + q;
+            if (l < kSlices) {
+#pragma unroll
+              for (int j = 0; j < kDrainCols; ++j) {
+                const long long w =
+                    (long long)__float2int_rn(__uint_as_float(v[q * kDrainCols + j]));
+                if (l <= 3)
+                  Rh[j] += w << (24 - 8 * l);
+                else
+                  Rl[j] += w << (48 - 8 * l);
+              }
+            }
           }
         }
         tc_fence_before();
@@ -627,6 +665,31 @@ int tile_count(long long m, long long n, bool sym) {
   constexpr int r = kTileM / kTileN;
   for (int tm = 0; tm < tmc; ++tm) t += tnc > r * tm ? tnc - r * tm : 0;
   return t;
+}
+// Tensor map of B's digit planes as 1 KB pieces (32 rows x 16 K of one
+// digit): dimension 0 the 128 8-byte words of a piece, dimension 1 the four
+// pieces of a digit's 128 rows (1 KB apart), dimension 2 the digits of all
+// blocks in order (4 KB apart).  A box {128, 1, kSlices} is the run of one
+// set's pieces over all digits of a block.
+cudaError_t b_pieces_map(const Planes& B, CUtensorMap* map) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return cudaErrorNotSupported;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[3] = {128, 4, (cuuint64_t)(B.nrb * B.nkc * kSlices)};
+  const cuuint64_t strides[2] = {1024, 4096};
+  const cuuint32_t box[3] = {128, 1, (cuuint32_t)kSlices};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, B.d, dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 }  // namespace
 
@@ -734,8 +797,11 @@ cudaError_t gemm_nt(const Planes& A, const Planes& B, double alpha, bool sym, bo
   a.err = err;
   const long long items = (long long)a.ntiles * a.nsplit;
   if (items < 1) return cudaSuccess;
+  CUtensorMap tmb;
+  e = b_pieces_map(B, &tmb);
+  if (e != cudaSuccess) return e;
   const unsigned grid = (unsigned)std::min<long long>(items, sm_count());
-  k_oz_mma<<<grid, kThreads, kStages * kStageBytes, s>>>(a);
+  k_oz_mma<<<grid, kThreads, kStages * kStageBytes, s>>>(a, tmb);
   e = cudaGetLastError();
   if (e != cudaSuccess || a.nsplit == 1) return e;
   const long long mn = A.rows * B.rows;

@@ -22,11 +22,14 @@
 //
 // Passes over shared memory.  The first y stage reads the plane from global
 // memory and the last one writes it there; x inverse stage A', the epilogue
-// and x forward stage A work on the same items and share one pass.  The row
-// stride is L + 1 elements, so that the threads of a half-warp on 16
-// different rows, or on 16 adjacent columns, touch different bank pairs.
-// Each block prefetches its next plane, psi_{j-1} and V into L2 while it
-// transforms the current one.
+// and x forward stage A work on the same items and share one pass.  In the
+// step pass (inverse, epilogue, forward) the last y stage of a plane and the
+// first y stage of the block's next plane also share one pass
+// (col_fwd_b_inv_b_next), so that the next plane's loads are in flight while
+// the current plane is written out.  The row stride is L + 1 elements, so
+// that the threads of a half-warp on 16 different rows, or on 16 adjacent
+// columns, touch different bank pairs.  Each block prefetches its next plane,
+// psi_{j-1} and V into L2 while it transforms the current one.
 #pragma once
 
 #include "sep_fftpass.cuh"
@@ -152,6 +155,62 @@ template <int L> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __
     C* q = g + (long long)(S::n1 * k2) * L + col;
 #pragma unroll
     for (int k1 = 0; k1 < S::n1; ++k1) q[(long long)k1 * L] = w[k1];
+  }
+}
+
+// forward stage B of the current plane (to gcur) and inverse stage B' of the
+// block's next plane (from gnext) in one pass: both stages have the items
+// (column, k2) at the same shared-memory positions and the same thread
+// mapping, so each thread first issues the loads of two next-plane items,
+// then transforms and stores its current items, then transforms the loaded
+// ones into the positions it has just read.  The next plane's load latency
+// runs under the current plane's last stage, and one barrier goes.
+template <int L>
+__device__ __forceinline__ void col_fwd_b_inv_b_next(C* pl, const C* tw, C* __restrict__ gcur,
+                                                     const C* __restrict__ gnext) {
+  using S = XyShape<L>;
+  constexpr int NI = L * S::n2;
+  constexpr int IB = 2;
+  for (int i0 = threadIdx.x; i0 < NI; i0 += IB * S::nt) {
+    C v[IB][S::n1];
+#pragma unroll
+    for (int t = 0; t < IB; ++t) {
+      const int i = i0 + t * S::nt;
+      if (NI % (IB * S::nt) == 0 || i < NI) {
+        const int col = i % L, k2 = i / L;
+        const C* q = gnext + (long long)(S::n1 * k2) * L + col;
+#pragma unroll
+        for (int k1 = 0; k1 < S::n1; ++k1) v[t][k1] = q[(long long)k1 * L];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < IB; ++t) {
+      const int i = i0 + t * S::nt;
+      if (NI % (IB * S::nt) == 0 || i < NI) {
+        const int col = i % L, k2 = i / L;
+        C* p = pl + S::n1 * k2 * S::rs + col;
+        C w[S::n1];
+#pragma unroll
+        for (int x1 = 0; x1 < S::n1; ++x1) w[x1] = p[x1 * S::rs];
+        Dft<S::n1, -1, float>::run(w);
+        C* q = gcur + (long long)(S::n1 * k2) * L + col;
+#pragma unroll
+        for (int k1 = 0; k1 < S::n1; ++k1) q[(long long)k1 * L] = w[k1];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < IB; ++t) {
+      const int i = i0 + t * S::nt;
+      if (NI % (IB * S::nt) == 0 || i < NI) {
+        const int col = i % L, k2 = i / L;
+        Dft<S::n1, +1, float>::run(v[t]);
+#pragma unroll
+        for (int n1 = 1; n1 < S::n1; ++n1) v[t][n1] = mulc<float>(v[t][n1], tw[(n1 * k2) % L]);
+        C* p = pl + S::n1 * k2 * S::rs + col;
+#pragma unroll
+        for (int n1 = 0; n1 < S::n1; ++n1) p[n1 * S::rs] = v[t][n1];
+      }
+    }
   }
 }
 
@@ -299,6 +358,7 @@ __global__ void __launch_bounds__(XyShape<L>::nt, XyShape<L>::min_blocks) xy_pla
     alpha = a.coefs[2 * a.step];
     beta = a.coefs[2 * a.step + 1];
   }
+  bool loaded = false;  // kInvEpiFwd: this plane's first stage ran with the previous plane's last
   for (long long p = blockIdx.x; p < planes; p += gridDim.x) {
     prefetch_epi(p);
     const long long goff = (p / B) * L * L;  // offset in one grid
@@ -307,8 +367,10 @@ __global__ void __launch_bounds__(XyShape<L>::nt, XyShape<L>::min_blocks) xy_pla
     if constexpr (MODE == kFwd) {
       xy::row_fwd_a_from<L>(pl, tw, src + off);  // x forward
     } else {
-      xy::col_inv_b_from<L>(pl, tw, a.data + off);  // y inverse
-      __syncthreads();
+      if (!loaded) {
+        xy::col_inv_b_from<L>(pl, tw, a.data + off);  // y inverse
+        __syncthreads();
+      }
       xy::col_inv_a<L>(pl);
       __syncthreads();
       xy::row_inv_b<L>(pl, tw);  // x inverse, epilogue (and x forward stage A)
@@ -322,7 +384,15 @@ __global__ void __launch_bounds__(XyShape<L>::nt, XyShape<L>::min_blocks) xy_pla
       __syncthreads();
       xy::col_fwd_a<L>(pl, tw);  // y forward
       __syncthreads();
-      xy::col_fwd_b_to<L>(pl, a.data + off);
+      const long long pn = p + gridDim.x;
+      if (MODE == kInvEpiFwd && pn < planes) {
+        // y forward stage B of this plane with y inverse stage B' of the next
+        const long long offn = (pn % B) * N + (pn / B) * L * L;
+        xy::col_fwd_b_inv_b_next<L>(pl, tw, a.data + off, a.data + offn);
+        loaded = true;
+      } else {
+        xy::col_fwd_b_to<L>(pl, a.data + off);
+      }
     }
   }
 }
