@@ -781,10 +781,27 @@ def run_sep(args):
         # like-for-like precision: the FP64 GPU filter against the FP64 CPU port
         extras["fp64"]["vs_cpu_port"] = extras["fp64"]["value"] / extras["cpu_baseline"]["value"]
 
+    heavy = not args.no_extras and rank == 0 and world == 1
+    if heavy:
+        # BASELINE configurations 2 and 4 on the same box, after the headline
+        # context has released its workspaces: 32 uneven nanocrystals in one
+        # launch against one after another, and the 4 nm sphere at 192^3
+        del start_d
+        ctx.close()
+        ctx = None
+        torch.cuda.empty_cache()
+        for key, fn in (("batched_uneven_32", lambda: batched_case(1, 1)),
+                        ("large_192", large_case)):
+            try:
+                extras[key] = fn()
+            except Exception as exc:  # an extra, not the bench line
+                extras[key] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.empty_cache()
+
     if rank == 0:
         # pack, first forward transform, per Newton step 2 (fused xy plane pass,
         # nx = ny = 128 in complex64) or 4 line passes, the accumulations, convert
-        fused = S.dims[0] == S.dims[1] and S.dims[0] in (64, 96, 128)
+        fused = S.dims[0] == S.dims[1] and S.dims[0] in (40, 48, 56, 64, 72, 80, 96, 112, 128)
         launches_step = 1 + 1 + (2 if fused else 4) * (nc - 1) + -(-nc // BLOCK_STEPS) + 1
         line = {"metric": "Hpsi applies/s at 128^3", "value": value, "unit": "applies/s",
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -799,12 +816,17 @@ def run_sep(args):
                 "clocks": clk.summary()}
         line.update(extras)
         print(json.dumps(line), flush=True)
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if dist:
         dist.destroy_process_group()
 
 
 def run_batched(args):
+    print(json.dumps(batched_case(args.steps, args.warmup)), flush=True)
+
+
+def batched_case(steps, warmup):
     """32 spheres, seeded radii U(1.0, 2.5) nm, grids rounded up to
     {48, 56, 64, 72, 80, 96, 112} at about 0.95 bohr, 16 start states x 4
     targets each, nc = 1024, complex64 filter.  One CUDA graph runs all 32
@@ -849,23 +871,23 @@ def run_batched(args):
 
     sequential()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         sequential()
-    t_seq = (time.perf_counter() - t0) / args.steps
+    t_seq = (time.perf_counter() - t0) / steps
     del dev
     torch.cuda.empty_cache()
     batch = sep.Batch([j["ctx"] for j in jobs], [ns] * len(jobs), ms, nc)
     for k, j in enumerate(jobs):
         batch.set_coefficients(k, j["an"], j["zn"], 4.0 / j["dE"], j["vmin"])
         batch.load_start(k, j["start"])
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         batch.run()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         batch.run()
-    t_bat = (time.perf_counter() - t0) / args.steps
+    t_bat = (time.perf_counter() - t0) / steps
     line = {"metric": "Hpsi applies/s, 32 uneven nanocrystals", "value": applies / t_bat,
-            "unit": "applies/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "unit": "applies/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
             "ms_per_step": 1e3 * t_bat, "higher_is_better": True, "dtype": "c64",
             "data": "synthetic",
             "config": {"workload": "32 CdSe-like spheres, radii U(1.0, 2.5) nm, 16 states x 4 "
@@ -874,11 +896,17 @@ def run_batched(args):
                        "tiles": [j["tiles"] for j in jobs][:4]},
             "sequential": {"value": applies / t_seq, "ms_per_step": 1e3 * t_seq},
             "speedup_one_launch_over_sequential": t_seq / t_bat}
-    print(json.dumps(line), flush=True)
     batch.close()
+    for j in jobs:
+        j["ctx"].close()
+    return line
 
 
 def run_large(args):
+    print(json.dumps(large_case()), flush=True)
+
+
+def large_case():
     """The large mixed-precision run: 4 nm CdSe-like sphere, 192^3 grid, 256
     start states x 8 targets, nc = 1024.  The complex64 filter's output (2048
     FP64 states, 116 GB) and ortho's second block of the same size share the
@@ -929,8 +957,8 @@ def run_large(args):
             "device_memory_used_gib": {"peak": max(u[0] for u in used) / 1024 if used else None,
                                        "total": used[0][1] / 1024 if used else None,
                                        "samples": len(used)}}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
 def main():

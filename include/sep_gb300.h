@@ -74,7 +74,7 @@ int sep_ctx_stream(sep_ctx *ctx, void **cuda_stream);             /* cudaStream_
 int sep_ctx_set_graphs(sep_ctx *ctx, int enable);
 /* Newton steps accumulated per pass over the step history (default 32). */
 int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
-/* Complex64 Newton steps on grids with nx = ny in {64, 96, 128} use one fused
+/* Complex64 Newton steps on grids with nx = ny in {40, 48, 56, 64, 72, 80, 96, 112, 128} use one fused
  * pass per z-plane for the x and y transforms and the epilogue (two grid
  * passes per step instead of four; same arithmetic per line).  enable = 0
  * selects the four line passes.  Default 1. */

@@ -19,29 +19,30 @@ int sm_count() {
 
 template <int L, int MODE>
 cudaError_t launch_xy(const PassArgs<float>& a, int B, cudaStream_t s) {
+  using T = XyTune<L>;
+  using S = XyShape<L, T::nt>;
   if (a.nz > 65535 || B < 1) return cudaErrorInvalidValue;
-  // 96^2 and 128^2 planes: one block per SM walks its planes; 64^2 planes
-  // (three blocks per SM) take one block each
+  // planes up to 64^2 take one block each (several per SM); larger planes:
+  // min_blocks blocks per SM walk the planes
   const long long planes = (long long)B * a.nz;
   if (planes > 0x7fffffffLL) return cudaErrorInvalidValue;
-  const int grid = (L <= 64 || planes < sm_count()) ? (int)planes : sm_count();
-  xy_plane_pass<L, MODE><<<grid, XyShape<L>::nt, XyShape<L>::smem_bytes, s>>>(a, B);
+  const long long walkers = (long long)sm_count() * T::min_blocks;
+  const int grid = (L <= 64 || planes < walkers) ? (int)planes : (int)walkers;
+  xy_plane_pass<L, MODE><<<grid, T::nt, S::smem_bytes, s>>>(a, B);
   return cudaGetLastError();
 }
 
 template <int L> cudaError_t prepare_len() {
+  constexpr int smem = (int)XyShape<L, XyTune<L>::nt>::smem_bytes;
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(xy_plane_pass<L, kFwd>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)XyShape<L>::smem_bytes)))
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
     return e;
   if ((e = cudaFuncSetAttribute(xy_plane_pass<L, kInvEpi>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)XyShape<L>::smem_bytes)))
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem)))
     return e;
   return cudaFuncSetAttribute(xy_plane_pass<L, kInvEpiFwd>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)XyShape<L>::smem_bytes);
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 template <int L>
@@ -54,10 +55,15 @@ cudaError_t launch_mode(int mode, const PassArgs<float>& a, int B, cudaStream_t 
 
 }  // namespace
 
+// the plane lengths with a plane pass: N1 = 8, a multiple of 8 rows, the
+// plane in one block's shared memory
+#define SEP_XY_LENGTHS(X) X(40) X(48) X(56) X(64) X(72) X(80) X(96) X(112) X(128)
+
 int xy_split_n1(int L) {
-  if (L == 64) return Split<64>::n1;
-  if (L == 96) return Split<96>::n1;
-  if (L == 128) return Split<128>::n1;
+#define SEP_XY_N1(LL) \
+  if (L == LL) return Split<LL>::n1;
+  SEP_XY_LENGTHS(SEP_XY_N1)
+#undef SEP_XY_N1
   return 0;
 }
 
@@ -66,9 +72,10 @@ bool xy_supported(const GridDev<float>& g) {
 }
 
 cudaError_t xy_prepare(const GridDev<float>& g) {
-  if (g.nx == 64) return prepare_len<64>();
-  if (g.nx == 96) return prepare_len<96>();
-  if (g.nx == 128) return prepare_len<128>();
+#define SEP_XY_PREP(LL) \
+  if (g.nx == LL) return prepare_len<LL>();
+  SEP_XY_LENGTHS(SEP_XY_PREP)
+#undef SEP_XY_PREP
   return cudaErrorInvalidValue;
 }
 
@@ -88,9 +95,10 @@ cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& 
   a.nx = g.nx;
   a.ny = g.ny;
   a.nz = g.nz;
-  if (g.nx == 64) return launch_mode<64>(mode, a, B, s);
-  if (g.nx == 96) return launch_mode<96>(mode, a, B, s);
-  if (g.nx == 128) return launch_mode<128>(mode, a, B, s);
+#define SEP_XY_RUN(LL) \
+  if (g.nx == LL) return launch_mode<LL>(mode, a, B, s);
+  SEP_XY_LENGTHS(SEP_XY_RUN)
+#undef SEP_XY_RUN
   return cudaErrorInvalidValue;
 }
 

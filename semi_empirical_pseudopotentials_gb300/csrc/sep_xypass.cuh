@@ -36,14 +36,49 @@
 
 namespace sep {
 
-template <int L> struct XyShape {
+// the plane pass's launch shape per length: threads per block and blocks per
+// SM.  A block needs about 128 registers per thread and its plane in shared
+// memory (13 KB at 40^2, 19 KB at 48^2, 25 KB at 56^2, 33 KB at 64^2, 42 KB
+// at 72^2, 52 KB at 80^2, 74 KB at 96^2, 102 KB at 112^2, 132 KB at 128^2).
+// Several blocks per SM let one block's transforms run while another waits
+// for memory; the shapes are the fastest measured per length (step pass on
+// 0.5 GB of grids, fraction of the copy bandwidth: 40^2 0.79, 48^2 0.79, 56^2
+// 0.75, 64^2 0.84, 72^2 0.79, 80^2 0.74, 96^2 0.76 against 0.57 with one
+// block of 512, 112^2 0.64, 128^2 0.73).  Only one 128^2 plane fits per SM.
+template <int L> struct XyTune {
+  static constexpr int nt = 512;
+  static constexpr int min_blocks = 1;
+};
+template <> struct XyTune<40> {
+  static constexpr int nt = 64, min_blocks = 8;
+};
+template <> struct XyTune<56> {
+  static constexpr int nt = 128, min_blocks = 4;
+};
+template <> struct XyTune<72> {
+  static constexpr int nt = 128, min_blocks = 4;
+};
+template <> struct XyTune<48> {
+  static constexpr int nt = 128, min_blocks = 4;
+};
+template <> struct XyTune<64> {
+  static constexpr int nt = 256, min_blocks = 3;
+};
+template <> struct XyTune<80> {
+  static constexpr int nt = 128, min_blocks = 4;
+};
+template <> struct XyTune<96> {
+  static constexpr int nt = 192, min_blocks = 2;
+};
+template <> struct XyTune<112> {
+  static constexpr int nt = 128, min_blocks = 2;
+};
+
+template <int L, int NT> struct XyShape {
   static constexpr int n1 = Split<L>::n1, n2 = Split<L>::n2;
   static constexpr int rs = L + 1;  // row stride (elements)
-  // threads per block and blocks per SM: a 64^2 plane (33 KB) leaves room
-  // for three blocks per SM
-  static constexpr int nt = L <= 64 ? 256 : 512;
-  static constexpr int min_blocks = L <= 64 ? 3 : 1;
-  static_assert(n1 == 8 && L % 16 == 0, "row groups of the epilogue step");
+  static constexpr int nt = NT;     // threads per block
+  static_assert(n1 == 8 && L % 8 == 0, "row groups of the epilogue step");
   static constexpr size_t smem_bytes = ((size_t)L * rs + L) * sizeof(cx<float>);
 };
 
@@ -63,9 +98,13 @@ __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes, int l
 }
 
 // row of group j of an x stage whose items are spread over N1 = 8 threads:
-// the two rows of a half-warp are 8 apart (16 banks apart with stride L + 1)
-__device__ __forceinline__ int row_of_group(int j) {
-  return (j & ~15) | ((j & 1) << 3) | ((j >> 1) & 7);
+// the two rows of a half-warp are 8 apart (16 banks apart with stride L + 1).
+// When L is 8 more than a multiple of 16, the last 8 rows pair rows 4 apart
+// (a bijection on those rows; some of their accesses share banks).
+template <int L> __device__ __forceinline__ int row_of_group(int j) {
+  constexpr int full = L & ~15;
+  if (L % 16 == 0 || j < full) return (j & ~15) | ((j & 1) << 3) | ((j >> 1) & 7);
+  return full + ((j & 1) << 2) + ((j >> 1) & 3);
 }
 
 // ---- y transforms: lines are the columns (element stride RS)
@@ -75,9 +114,9 @@ __device__ __forceinline__ int row_of_group(int j) {
 // conjugate twiddle, back to the same positions in shared memory.  Adjacent
 // threads on adjacent columns; a thread's items (four when they divide
 // evenly, else two at a time) are loaded before any is transformed.
-template <int L>
+template <int L, int NT>
 __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __restrict__ g) {
-  using S = XyShape<L>;
+  using S = XyShape<L, NT>;
   constexpr int NI = L * S::n2;
   constexpr int IB = NI % (4 * S::nt) == 0 ? 4 : 2;  // items loaded per batch
   for (int i0 = threadIdx.x; i0 < NI; i0 += IB * S::nt) {
@@ -110,8 +149,8 @@ __device__ __forceinline__ void col_inv_b_from(C* pl, const C* tw, const C* __re
 
 // inverse stage A': item (column, n1): positions n1 + N1 k2 -> inverse DFT_N2;
 // element n1 + N1 n2 at its natural position
-template <int L> __device__ __forceinline__ void col_inv_a(C* pl) {
-  using S = XyShape<L>;
+template <int L, int NT> __device__ __forceinline__ void col_inv_a(C* pl) {
+  using S = XyShape<L, NT>;
   for (int i = threadIdx.x; i < L * S::n1; i += S::nt) {
     const int col = i % L, n1 = i / L;
     C* p = pl + n1 * S::rs + col;
@@ -125,8 +164,8 @@ template <int L> __device__ __forceinline__ void col_inv_a(C* pl) {
 }
 
 // forward stage A: item (column, x1): positions x1 + N1 x2 -> DFT_N2, twiddle
-template <int L> __device__ __forceinline__ void col_fwd_a(C* pl, const C* tw) {
-  using S = XyShape<L>;
+template <int L, int NT> __device__ __forceinline__ void col_fwd_a(C* pl, const C* tw) {
+  using S = XyShape<L, NT>;
   for (int i = threadIdx.x; i < L * S::n1; i += S::nt) {
     const int col = i % L, x1 = i / L;
     C* p = pl + x1 * S::rs + col;
@@ -143,8 +182,8 @@ template <int L> __device__ __forceinline__ void col_fwd_a(C* pl, const C* tw) {
 
 // forward stage B to global memory: item (column, k2): positions x1 + N1 k2
 // -> DFT_N1; element k2 + N2 k1 to position k1 + N1 k2 of g
-template <int L> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __restrict__ g) {
-  using S = XyShape<L>;
+template <int L, int NT> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __restrict__ g) {
+  using S = XyShape<L, NT>;
   for (int i = threadIdx.x; i < L * S::n2; i += S::nt) {
     const int col = i % L, k2 = i / L;
     const C* p = pl + S::n1 * k2 * S::rs + col;
@@ -165,10 +204,10 @@ template <int L> __device__ __forceinline__ void col_fwd_b_to(const C* pl, C* __
 // then transforms and stores its current items, then transforms the loaded
 // ones into the positions it has just read.  The next plane's load latency
 // runs under the current plane's last stage, and one barrier goes.
-template <int L>
+template <int L, int NT>
 __device__ __forceinline__ void col_fwd_b_inv_b_next(C* pl, const C* tw, C* __restrict__ gcur,
                                                      const C* __restrict__ gnext) {
-  using S = XyShape<L>;
+  using S = XyShape<L, NT>;
   constexpr int NI = L * S::n2;
   constexpr int IB = 2;
   for (int i0 = threadIdx.x; i0 < NI; i0 += IB * S::nt) {
@@ -218,8 +257,8 @@ __device__ __forceinline__ void col_fwd_b_inv_b_next(C* pl, const C* tw, C* __re
 
 // inverse stage B': item (row, k2): positions k1 + N1 k2 (elements k2 + N2 k1)
 // -> inverse DFT_N1, conjugate twiddle
-template <int L> __device__ __forceinline__ void row_inv_b(C* pl, const C* tw) {
-  using S = XyShape<L>;
+template <int L, int NT> __device__ __forceinline__ void row_inv_b(C* pl, const C* tw) {
+  using S = XyShape<L, NT>;
   for (int i = threadIdx.x; i < L * S::n2; i += S::nt) {
     const int row = i % L, k2 = i / L;
     C* p = pl + row * S::rs + S::n1 * k2;
@@ -236,8 +275,8 @@ template <int L> __device__ __forceinline__ void row_inv_b(C* pl, const C* tw) {
 
 // forward stage B: item (row, k2): positions x1 + N1 k2 -> DFT_N1; element
 // k2 + N2 k1 stays at position k1 + N1 k2
-template <int L> __device__ __forceinline__ void row_fwd_b(C* pl) {
-  using S = XyShape<L>;
+template <int L, int NT> __device__ __forceinline__ void row_fwd_b(C* pl) {
+  using S = XyShape<L, NT>;
   for (int i = threadIdx.x; i < L * S::n2; i += S::nt) {
     const int row = i % L, k2 = i / L;
     C* p = pl + row * S::rs + S::n1 * k2;
@@ -255,16 +294,16 @@ template <int L> __device__ __forceinline__ void row_fwd_b(C* pl) {
 // are also the inputs of forward item (row, x1 = n1).  psi_{j-1}, V and psi_j
 // (plane offsets off in the batch, goff in one grid) are accessed at those
 // elements: eight threads cover N1 = 8 adjacent elements (64 bytes) of a row.
-template <int L, bool FWD>
+template <int L, int NT, bool FWD>
 __device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs<float>& a,
                                               long long off, long long goff, float alpha,
                                               float beta) {
-  using S = XyShape<L>;
+  using S = XyShape<L, NT>;
   const C* __restrict__ pin = a.psi_in ? a.psi_in + off : nullptr;
   const float* __restrict__ pv = a.pot + goff;
   C* __restrict__ pout = a.psi_out + off;
   for (int i = threadIdx.x; i < L * 8; i += S::nt) {
-    const int n1 = i & 7, row = row_of_group(i >> 3);
+    const int n1 = i & 7, row = row_of_group<L>(i >> 3);
     const long long g0 = (long long)row * L + n1;
     // the item's psi_{j-1} and V are requested before its transform, so
     // their latency runs under the shared-memory reads and the DFT
@@ -298,11 +337,11 @@ __device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs
 }
 
 // x forward stage A from global memory (natural order): item (row, x1)
-template <int L>
+template <int L, int NT>
 __device__ __forceinline__ void row_fwd_a_from(C* pl, const C* tw, const C* __restrict__ g) {
-  using S = XyShape<L>;
+  using S = XyShape<L, NT>;
   for (int i = threadIdx.x; i < L * 8; i += S::nt) {
-    const int x1 = i & 7, row = row_of_group(i >> 3);
+    const int x1 = i & 7, row = row_of_group<L>(i >> 3);
     const C* q = g + (long long)row * L + x1;
     C v[S::n2];
 #pragma unroll
@@ -327,10 +366,10 @@ __device__ __forceinline__ void row_fwd_a_from(C* pl, const C* tw, const C* __re
 // MODE: kFwd (x and y forward of src, or of data, natural order in),
 // kInvEpi (y and x inverse + epilogue), kInvEpiFwd (and the forward
 // transforms of the result).
-template <int L, int MODE>
-__global__ void __launch_bounds__(XyShape<L>::nt, XyShape<L>::min_blocks) xy_plane_pass(PassArgs<float> a, int B) {
+template <int L, int MODE, int NT = XyTune<L>::nt, int MINB = XyTune<L>::min_blocks>
+__global__ void __launch_bounds__(NT, MINB) xy_plane_pass(PassArgs<float> a, int B) {
   using C = cx<float>;
-  using S = XyShape<L>;
+  using S = XyShape<L, NT>;
   extern __shared__ __align__(16) unsigned char xy_smem[];
   C* pl = reinterpret_cast<C*>(xy_smem);
   C* tw = pl + L * S::rs;
@@ -365,33 +404,33 @@ __global__ void __launch_bounds__(XyShape<L>::nt, XyShape<L>::min_blocks) xy_pla
     const long long off = (p % B) * N + goff;
     __syncthreads();  // the previous plane's last stage has read the plane
     if constexpr (MODE == kFwd) {
-      xy::row_fwd_a_from<L>(pl, tw, src + off);  // x forward
+      xy::row_fwd_a_from<L, NT>(pl, tw, src + off);  // x forward
     } else {
       if (!loaded) {
-        xy::col_inv_b_from<L>(pl, tw, a.data + off);  // y inverse
+        xy::col_inv_b_from<L, NT>(pl, tw, a.data + off);  // y inverse
         __syncthreads();
       }
-      xy::col_inv_a<L>(pl);
+      xy::col_inv_a<L, NT>(pl);
       __syncthreads();
-      xy::row_inv_b<L>(pl, tw);  // x inverse, epilogue (and x forward stage A)
+      xy::row_inv_b<L, NT>(pl, tw);  // x inverse, epilogue (and x forward stage A)
       __syncthreads();
-      xy::row_inv_a_epi<L, MODE == kInvEpiFwd>(pl, tw, a, off, goff, alpha, beta);
+      xy::row_inv_a_epi<L, NT, MODE == kInvEpiFwd>(pl, tw, a, off, goff, alpha, beta);
     }
     prefetch_data(p + gridDim.x);
     if constexpr (MODE != kInvEpi) {
       __syncthreads();
-      xy::row_fwd_b<L>(pl);
+      xy::row_fwd_b<L, NT>(pl);
       __syncthreads();
-      xy::col_fwd_a<L>(pl, tw);  // y forward
+      xy::col_fwd_a<L, NT>(pl, tw);  // y forward
       __syncthreads();
       const long long pn = p + gridDim.x;
       if (MODE == kInvEpiFwd && pn < planes) {
         // y forward stage B of this plane with y inverse stage B' of the next
         const long long offn = (pn % B) * N + (pn / B) * L * L;
-        xy::col_fwd_b_inv_b_next<L>(pl, tw, a.data + off, a.data + offn);
+        xy::col_fwd_b_inv_b_next<L, NT>(pl, tw, a.data + off, a.data + offn);
         loaded = true;
       } else {
-        xy::col_fwd_b_to<L>(pl, a.data + off);
+        xy::col_fwd_b_to<L, NT>(pl, a.data + off);
       }
     }
   }

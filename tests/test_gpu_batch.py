@@ -66,14 +66,15 @@ def test_autotuned_tile_shapes_give_identical_results(precision):
     assert np.array_equal(a, c)
 
 
-@pytest.mark.parametrize("dims", [(64, 64, 24), (96, 96, 24), (128, 128, 16), (96, 96, 64),
-                                  (128, 128, 64)])
+@pytest.mark.parametrize("dims", [(40, 40, 24), (48, 48, 40), (56, 56, 32), (64, 64, 24),
+                                  (96, 96, 24), (128, 128, 16), (72, 72, 128), (80, 80, 128),
+                                  (96, 96, 64), (112, 112, 128), (128, 128, 64)])
 def test_fused_xy_plane_pass_equals_the_line_passes(dims):
     """The complex64 Newton step with the fused xy plane pass does the same
     arithmetic per line as the four line passes: the filters are equal.  With
-    nz = 64 the 3 pairs have 192 planes, more than the GPU has SMs, so blocks
-    walk several planes and the last y stage of a plane runs fused with the
-    first y stage of the next."""
+    nz = 64 or 128 the 3 pairs have 192 or 384 planes, more than the blocks
+    that walk them, so the last y stage of a plane runs fused with the first y
+    stage of the next."""
     ctx, pot, dv, npts = _job(dims, 3, "mixed")
     vmin = float(pot.min())
     nc, dE = 70, 40.0
