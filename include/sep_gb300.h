@@ -396,7 +396,8 @@ int sep_read_grid_source(const char *path, long *ngrid);
  * sep_bulk_bands: params = ntype x {a0, a1, a2, a3} of
  *   v(q) = a0 (q^2 - a1) / (a2 exp(a3 q^2) + 1) (hamiltonian.c:91-94);
  *   bands = nk x nev lowest eigenvalues in eV (fit.c:71-97: V once, H_k for
- *   all k-points, one batched Hermitian eigensolve).
+ *   all k-points, one batched Hermitian eigensolve of the lowest nev + 16
+ *   eigenpairs).
  * sep_bulk_bands_backward: given dL/dE (nk x nev, per eV), writes
  *   dL/dparams (ntype x 4) by Hellmann-Feynman (no reference counterpart:
  *   the reference fits by Monte Carlo, fit.c:9-69), and the bands when
@@ -406,20 +407,36 @@ int sep_read_grid_source(const char *path, long *ngrid);
  *   from degenerate perturbation theory on each cluster (the eigenvalues of
  *   U_c^H dV/dtheta U_c, up to 16 bands per cluster; bands past nev in a
  *   cluster count with dL/dE = 0).
- * sep_bulk_solver_path: 1 when the batched eigensolver ran, 0 when the
- *   matrices went one per call, -1 before the first solve.
- * sep_bulk_set_solver: 1 (default) = the batched eigensolver, one matrix per
- *   call where it declines the size; 0 = one matrix per call. */
+ * sep_bulk_solver_path: 2 when the library's batched solver ran, 1 when
+ *   cuSOLVER's batched eigensolver ran, 0 when the matrices went to cuSOLVER
+ *   one per call, -1 before the first solve.
+ * sep_bulk_set_eigensolver: 1 (default) = the library's batched solver (one
+ *   CTA per k-point, up to 512 plane waves; larger bases use cuSOLVER);
+ *   0 = cuSOLVER.
+ * sep_bulk_set_solver: for cuSOLVER, 1 (default) = its batched eigensolver,
+ *   one matrix per call where it declines the size; 0 = one matrix per call. */
 typedef struct sep_bulk sep_bulk;
 int sep_bulk_basis(const double cell[9], double max_ke, long cap, long *nbv, double *g);
 int sep_bulk_create(long nbv, const double *g, long natom, const double *tau, const int *types,
                     long ntype, long nk, const double *kpts, double ke_scale, long nev,
                     sep_bulk **out);
 int sep_bulk_bands(sep_bulk *b, const double *params, double *bands);
+/* sep_bulk_bands that also keeps the eigenvectors: a following
+ * sep_bulk_bands_backward with the same params reuses this solve. */
+int sep_bulk_bands_keep(sep_bulk *b, const double *params, double *bands);
 int sep_bulk_bands_backward(sep_bulk *b, const double *params, const double *dl_de,
                             double *bands, double *dl_dparams);
 int sep_bulk_solver_path(sep_bulk *b, int *batched);
 int sep_bulk_set_solver(sep_bulk *b, int batched);
+int sep_bulk_set_eigensolver(sep_bulk *b, int mode);
+/* The library's batched Hermitian solver on host arrays: a = nmat matrices
+ * of order n (2 <= n <= 512), complex interleaved (re, im), column-major,
+ * both triangles; w = nmat x nw lowest eigenvalues ascending (nw <= 64);
+ * with vectors, v = nmat x nw unit eigenvectors of n complex each (the
+ * matrix's first nw columns).  Replaces one zheev per k-point
+ * (pseudopotFitting/diag.c:12-48) keeping the lowest bands (fit.c:86-88). */
+int sep_hermitian_lowest(const double *a, long n, long nmat, long nw, int vectors, double *w,
+                         double *v);
 int sep_bulk_destroy(sep_bulk *b);
 
 /* ---- spin-orbit operator of the spinor filter (spinors/filterSpinors/) ----

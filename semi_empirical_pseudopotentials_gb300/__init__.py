@@ -14,10 +14,12 @@ from .binding import (  # noqa: F401
     device_count,
     form_factor_backward,
     form_factor_table,
+    hermitian_lowest,
     ksqr,
     lib,
     start_states,
 )
 
-__all__ = ["Batch", "Context", "SepError", "coefficients", "device_count", "form_factor_backward", "form_factor_table", "ksqr",
+__all__ = ["Batch", "Context", "SepError", "coefficients", "device_count", "form_factor_backward", "form_factor_table",
+           "hermitian_lowest", "ksqr",
            "lib", "start_states"]

@@ -118,9 +118,12 @@ def lib():
         L.sep_bulk_create.argtypes = [C.c_long, dp, C.c_long, dp, ip, C.c_long, C.c_long, dp,
                                       C.c_double, C.c_long, C.POINTER(vp)]
         L.sep_bulk_bands.argtypes = [vp, dp, dp]
+        L.sep_bulk_bands_keep.argtypes = [vp, dp, dp]
         L.sep_bulk_bands_backward.argtypes = [vp, dp, dp, dp, dp]
         L.sep_bulk_solver_path.argtypes = [vp, ip]
         L.sep_bulk_set_solver.argtypes = [vp, C.c_int]
+        L.sep_bulk_set_eigensolver.argtypes = [vp, C.c_int]
+        L.sep_hermitian_lowest.argtypes = [dp, C.c_long, C.c_long, C.c_long, C.c_int, dp, dp]
         L.sep_bulk_destroy.argtypes = [vp]
         L.sep_spinor_vso.argtypes = [dp, C.c_long, C.c_long, C.c_long, vp, lp, C.c_double,
                                      C.c_double, C.c_int, dp, dp]
@@ -192,6 +195,26 @@ def form_factor_backward(params, vol_per_atom, dtab):
     g = np.empty(4)
     _check(lib().sep_form_factor_backward(_p(a), vol_per_atom, _p(d), _p(g)))
     return g
+
+
+def hermitian_lowest(a, nw, vectors=True):
+    """The lowest nw eigenpairs of each Hermitian matrix a[m] (nmat x n x n,
+    complex) with the library's batched solver: (w [nmat, nw], v [nmat, n,
+    nw] or None), the columns of v unit eigenvectors."""
+    a = np.asarray(a, dtype=np.complex128)
+    if a.ndim == 2:
+        a = a[None]
+    nmat, n, n2 = a.shape
+    if n != n2:
+        raise ValueError("square matrices")
+    # column-major per matrix: the transpose of each row-major matrix
+    at = np.ascontiguousarray(np.transpose(a, (0, 2, 1)))
+    w = np.empty((nmat, nw))
+    v = np.empty((nmat, nw, n), dtype=np.complex128) if vectors else None
+    _check(lib().sep_hermitian_lowest(at.view(np.float64).ctypes.data_as(dp), n, nmat, nw,
+                                      1 if vectors else 0, _p(w),
+                                      v.view(np.float64).ctypes.data_as(dp) if vectors else None))
+    return w, (np.transpose(v, (0, 2, 1)) if vectors else None)
 
 
 class Context:

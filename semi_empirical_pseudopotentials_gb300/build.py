@@ -28,7 +28,7 @@ CUDA_UNITS = ["sep_pass_f64.cu", "sep_pass_f32.cu", "sep_pass_f64_v1.cu", "sep_p
               "sep_kernels.cu", "sep_ctx.cu",
               "sep_api.cu", "sep_vbuild.cu", "sep_noalloc.cu",
               "sep_ozaki.cu", "sep_bulk.cu", "sep_spinor.cu", "sep_spinor_path.cu",
-              "sep_eigh.cu"]
+              "sep_eigh.cu", "sep_heevb.cu"]
 CXX_UNITS = ["sep_host.cpp", "sep_adjoint.cpp", "sep_io.cpp", "sep_spinor_host.cpp"]
 
 

@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -224,11 +225,14 @@ class BulkCrystal:
         ap = np.asarray(atom_params, dtype=np.float64)
         return np.ascontiguousarray([ap[self.crystal.symbols.index(s)] for s in self.types_of])
 
-    def bands(self, type_params):
+    def bands(self, type_params, keep_vectors=False):
+        """nk x nev bands in eV.  keep_vectors: also keep the eigenvectors, so
+        that backward() with the same parameters needs no second solve."""
         p = np.ascontiguousarray(type_params, dtype=np.float64).reshape(-1, 4)
         out = np.zeros((self.nk, self.nev))
         dp = C.POINTER(C.c_double)
-        _check(lib().sep_bulk_bands(self._h, p.ctypes.data_as(dp), out.ctypes.data_as(dp)))
+        f = lib().sep_bulk_bands_keep if keep_vectors else lib().sep_bulk_bands
+        _check(f(self._h, p.ctypes.data_as(dp), out.ctypes.data_as(dp)))
         return out
 
     def backward(self, type_params, dl_de):
@@ -243,8 +247,15 @@ class BulkCrystal:
         return out, grad
 
     def set_solver(self, batched):
-        """True: the batched eigensolver (default); False: one matrix per call."""
+        """cuSOLVER: True its batched eigensolver (default), False one matrix per call."""
         _check(lib().sep_bulk_set_solver(self._h, 1 if batched else 0))
+
+    def set_eigensolver(self, mode):
+        """"native" (default): the library's batched solver of the lowest bands;
+        "cusolver": cuSOLVER (see set_solver)."""
+        if mode not in ("native", "cusolver"):
+            raise ValueError("eigensolver: 'native' or 'cusolver'")
+        _check(lib().sep_bulk_set_eigensolver(self._h, 1 if mode == "native" else 0))
 
     @property
     def solver_path(self):
@@ -286,8 +297,18 @@ class BulkFit:
             out.append(np.array([fit_atom_params(self.fit, theta, ci, s) for s in bc.types_of]))
         return out
 
+    def _each_crystal(self, fn, theta):
+        """fn(ci, crystal, params) for every crystal at once: each crystal has
+        its own stream, and the library calls release the GIL, so the
+        crystals' solves share the GPU."""
+        jobs = list(zip(range(len(self.crystals)), self.crystals, self.crystal_params(theta)))
+        if len(jobs) == 1:
+            return [fn(*jobs[0])]
+        with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+            return list(ex.map(lambda j: fn(*j), jobs))
+
     def band_structures(self, theta):
-        return [bc.bands(p) for bc, p in zip(self.crystals, self.crystal_params(theta))]
+        return self._each_crystal(lambda ci, bc, p: bc.bands(p), theta)
 
     def _mse_terms(self, ci, b, weighted=True):
         exp = self.fit.crystals[ci].exp_bands
@@ -308,10 +329,14 @@ class BulkFit:
         theta = np.asarray(theta, dtype=np.float64)
         nbs = len(self.crystals)
         total, grad = 0.0, np.zeros_like(theta)
-        for ci, (bc, p) in enumerate(zip(self.crystals, self.crystal_params(theta))):
-            b = bc.bands(p)
+
+        def one(ci, bc, p):  # one solve: the bands, then the gradient from its eigenvectors
+            b = bc.bands(p, keep_vectors=True)
             mse, dl_de = self._mse_terms(ci, b)
             _, gp = bc.backward(p, dl_de / nbs)
+            return mse, gp
+
+        for ci, (bc, (mse, gp)) in enumerate(zip(self.crystals, self._each_crystal(one, theta))):
             total += mse / nbs
             for t, s in enumerate(bc.types_of):
                 e = self.fit.elements.index(s)

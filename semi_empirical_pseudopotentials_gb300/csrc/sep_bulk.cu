@@ -10,9 +10,12 @@
 //      hamiltonian.c:91-94) on the GPU, once for all k-points;
 //   2. assembles H_k = V + diag(s |k + G_j|^2 / 2) for every k-point at once
 //      (hamiltonian.c:11-52), column-major nbv x nbv complex;
-//   3. diagonalises all nk matrices in one batched cuSOLVER call
-//      (cusolverDnXsyevBatched; per-matrix Zheevd where the batched routine
-//      declines the size) in place of one zheev per k-point (diag.c:12-48);
+//   3. finds the lowest nev (+ 16, for degenerate clusters that reach past
+//      band nev) eigenpairs of all nk matrices at once with the library's
+//      batched Hermitian solver (sep_heevb.cu: one CTA per matrix), in place
+//      of one zheev per k-point (diag.c:12-48); cuSOLVER's batched routine
+//      (cusolverDnXsyevBatched, or Zheevd per matrix where it declines the
+//      size) stays selectable;
 //   4. keeps the lowest nev eigenvalues of each in eV (fit.c:86-88).
 // The reference's fit searches the parameters by Monte Carlo (fit.c:9-69);
 // sep_bulk_bands_backward gives the gradient instead:
@@ -30,6 +33,7 @@
 #include <vector>
 
 #include "../../include/sep_gb300.h"
+#include "sep_heevb.cuh"
 
 namespace sep {
 void set_error(const std::string& msg);
@@ -66,6 +70,14 @@ struct sep_bulk {
   size_t dwork_bytes = 0;
   std::vector<char> hwork;
   int batched = -1;           // -1 untried, 1 batched routine, 0 per-matrix
+  int native = 1;             // 1: the library's batched solver (sep_heevb.cu), 0: cuSOLVER
+  int path = -1;              // last solve: 2 library, 1 cuSOLVER batched, 0 per matrix
+  void* hbwork = nullptr;
+  size_t hbwork_bytes = 0;
+  // the last solve: its parameters, and whether b->h holds its eigenvectors
+  // (a backward call with the same parameters reuses them)
+  std::vector<double> last_params;
+  bool last_vectors = false;
 };
 
 namespace {
@@ -399,6 +411,31 @@ unsigned blocks_for(long n) { return (unsigned)((n + kThreads - 1) / kThreads); 
 
 // eigenvalues (and eigenvectors when vectors != 0) of the nk matrices in b->h
 int eig_all(sep_bulk* b, bool vectors) {
+  // the library's solver: the lowest nev + kMaxCluster eigenpairs (NaN after
+  // them in b->w), enough for the bands and for any cluster of up to
+  // kMaxCluster bands that starts below band nev
+  const int nwant = (int)std::min<long>(b->nbv, b->nev + kMaxCluster);
+  if (b->native && sep::hb::supported((int)b->nbv, nwant)) {
+    const size_t need = sep::hb::work_bytes((int)b->nbv, (int)b->nk, nwant);
+    if (need > b->hbwork_bytes) {
+      if (b->hbwork) cudaFree(b->hbwork);
+      b->hbwork = nullptr;
+      b->hbwork_bytes = 0;
+      BK(cudaMalloc(&b->hbwork, need));
+      b->hbwork_bytes = need;
+    }
+    BK(sep::hb::lowest(reinterpret_cast<double2*>(b->h), (int)b->nbv, (int)b->nk, nwant, vectors,
+                       b->w, b->hbwork, b->stream));
+    b->path = 2;
+    if (vectors) {
+      int bad = 0;
+      BK(sep::hb::failed_vectors(b->hbwork, (int)b->nbv, (int)b->nk, nwant, &bad, b->stream));
+      if (bad)
+        return fail(SEP_ERR_SOLVER, "sep_bulk: inverse iteration did not converge for " +
+                                        std::to_string(bad) + " eigenvector(s)");
+    }
+    return SEP_OK;
+  }
   const cusolverEigMode_t jobz = vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR;
   const cublasFillMode_t uplo = CUBLAS_FILL_MODE_LOWER;
   const int64_t n = b->nbv;
@@ -422,6 +459,7 @@ int eig_all(sep_bulk* b, bool vectors) {
           b->info, (int64_t)b->nk);
       if (r == CUSOLVER_STATUS_SUCCESS) {
         b->batched = 1;
+        b->path = 1;
         return SEP_OK;
       }
       if (b->batched == 1) BS(r);
@@ -445,6 +483,7 @@ int eig_all(sep_bulk* b, bool vectors) {
   for (long k = 0; k < b->nk; ++k)
     BS(cusolverDnZheevd(b->solver, jobz, uplo, (int)n, b->h + k * n * n, (int)n, b->w + k * n,
                         (cuDoubleComplex*)b->dwork, lwork, b->info + k));
+  b->path = 0;
   return SEP_OK;
 }
 
@@ -466,6 +505,11 @@ int check_info(sep_bulk* b) {
 // potential, assembly and the eigensolver for params (ntype x 4, host)
 int solve(sep_bulk* b, const double* params, bool vectors) {
   BK(cudaSetDevice(b->device));
+  const size_t np = (size_t)(4 * b->ntype);
+  if (b->last_params.size() == np && (b->last_vectors || !vectors) &&
+      std::equal(params, params + np, b->last_params.begin()))
+    return SEP_OK;  // b->w (and b->h) already hold this solve
+  b->last_params.clear();
   BK(cudaMemcpyAsync(b->params, params, sizeof(double) * 4 * b->ntype, cudaMemcpyHostToDevice,
                      b->stream));
   const long n2 = b->nbv * b->nbv;
@@ -482,7 +526,10 @@ int solve(sep_bulk* b, const double* params, bool vectors) {
     r = eig_all(b, vectors);
   }
   if (r != SEP_OK) return r == kRetry ? fail(SEP_ERR_SOLVER, "sep_bulk: eigensolver retry") : r;
-  return check_info(b);
+  if (b->path != 2 && (r = check_info(b)) != SEP_OK) return r;
+  b->last_params.assign(params, params + np);
+  b->last_vectors = vectors;
+  return SEP_OK;
 }
 
 template <typename T> int dalloc(T** p, size_t count) {
@@ -588,9 +635,9 @@ int sep_bulk_create(long nbv, const double* g, long natom, const double* tau, co
   return SEP_OK;
 }
 
-int sep_bulk_bands(sep_bulk* b, const double* params, double* bands) {
+static int bands_impl(sep_bulk* b, const double* params, double* bands, bool vectors) {
   if (!b || !params || !bands) return fail(SEP_ERR_ARG, "sep_bulk_bands: bad arguments");
-  int r = solve(b, params, false);
+  int r = solve(b, params, vectors);
   if (r != SEP_OK) return r;
   k_bulk_take<<<blocks_for(b->nk * b->nev), kThreads, 0, b->stream>>>(b->w, b->nbv, b->nk, b->nev,
                                                                        b->bands);
@@ -599,6 +646,14 @@ int sep_bulk_bands(sep_bulk* b, const double* params, double* bands) {
                      b->stream));
   BK(cudaStreamSynchronize(b->stream));
   return SEP_OK;
+}
+
+int sep_bulk_bands(sep_bulk* b, const double* params, double* bands) {
+  return bands_impl(b, params, bands, false);
+}
+
+int sep_bulk_bands_keep(sep_bulk* b, const double* params, double* bands) {
+  return bands_impl(b, params, bands, true);
 }
 
 int sep_bulk_bands_backward(sep_bulk* b, const double* params, const double* dl_de, double* bands,
@@ -746,13 +801,74 @@ int sep_bulk_bands_backward(sep_bulk* b, const double* params, const double* dl_
 
 int sep_bulk_solver_path(sep_bulk* b, int* batched) {
   if (!b || !batched) return fail(SEP_ERR_ARG, "sep_bulk_solver_path: bad arguments");
-  *batched = b->batched;
+  *batched = b->path;
+  return SEP_OK;
+}
+
+int sep_hermitian_lowest(const double* a, long n, long nmat, long nw, int vectors, double* w,
+                         double* v) {
+  if (!a || !w || (vectors && !v) || nmat < 1 || !sep::hb::supported((int)n, (int)nw))
+    return fail(SEP_ERR_ARG, "sep_hermitian_lowest: 2 <= n <= 512, 1 <= nw <= min(n, 64), nmat >= 1");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return fail(SEP_ERR_NO_DEVICE, "sep_hermitian_lowest: no CUDA device");
+  }
+  const size_t nn = (size_t)n * n * nmat;
+  double2* dA = nullptr;
+  double* dw = nullptr;
+  void* work = nullptr;
+  cudaStream_t s = nullptr;
+  auto done = [&](int r) {
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(dA);
+    cudaFree(dw);
+    cudaFree(work);
+    if (s) cudaStreamDestroy(s);
+    return r;
+  };
+  const size_t wb = sep::hb::work_bytes((int)n, (int)nmat, (int)nw);
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&dA, sizeof(double2) * nn) != cudaSuccess ||
+      cudaMalloc(&dw, sizeof(double) * n * nmat) != cudaSuccess || cudaMalloc(&work, wb) != cudaSuccess) {
+    cudaGetLastError();
+    return done(fail(SEP_ERR_NOMEM, "sep_hermitian_lowest: device allocation"));
+  }
+  cudaError_t e = cudaMemcpyAsync(dA, a, sizeof(double2) * nn, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = sep::hb::lowest(dA, (int)n, (int)nmat, (int)nw, vectors != 0, dw, work, s);
+  for (long m = 0; e == cudaSuccess && m < nmat; ++m) {
+    e = cudaMemcpyAsync(w + m * nw, dw + m * n, sizeof(double) * nw, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && vectors)
+      e = cudaMemcpyAsync(v + 2 * m * nw * n, dA + (size_t)m * n * n, sizeof(double2) * nw * n,
+                          cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    char m[200];
+    snprintf(m, sizeof m, "sep_hermitian_lowest: CUDA error %d (%s)", (int)e, cudaGetErrorString(e));
+    return done(fail(SEP_ERR_CUDA, m));
+  }
+  if (vectors) {
+    int bad = 0;
+    if (sep::hb::failed_vectors(work, (int)n, (int)nmat, (int)nw, &bad, s) != cudaSuccess)
+      return done(fail(SEP_ERR_CUDA, "sep_hermitian_lowest: status read"));
+    if (bad) return done(fail(SEP_ERR_SOLVER, "sep_hermitian_lowest: inverse iteration did not converge"));
+  }
+  return done(SEP_OK);
+}
+
+int sep_bulk_set_eigensolver(sep_bulk* b, int mode) {
+  if (!b || mode < 0 || mode > 1)
+    return fail(SEP_ERR_ARG, "sep_bulk_set_eigensolver: mode 0 (cuSOLVER) or 1 (library)");
+  b->native = mode;
+  b->last_params.clear();
   return SEP_OK;
 }
 
 int sep_bulk_set_solver(sep_bulk* b, int batched) {
   if (!b || batched < 0 || batched > 1) return fail(SEP_ERR_ARG, "sep_bulk_set_solver: mode 0 or 1");
   b->batched = batched ? -1 : 0;
+  b->last_params.clear();
   return SEP_OK;
 }
 
@@ -762,7 +878,7 @@ int sep_bulk_destroy(sep_bulk* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   void* bufs[] = {b->g, b->tau, b->types, b->kpts, b->params, b->v, b->h, b->wmat, b->w,
                   b->bands, b->dlde, b->partials, b->grad, b->info, b->dwork, b->clu,
-                  b->cluy, b->clum};
+                  b->cluy, b->clum, b->hbwork};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->sparams) cusolverDnDestroyParams(b->sparams);

@@ -759,7 +759,15 @@ cudaError_t solve(double* A, int n, double* w, double* work, cudaStream_t s, int
     EK(cudaGetDevice(&dev));
     EK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem = sizeof(double) * (2 * (size_t)n + kT / 32);
-    EK(cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the limit is the device's opt-in maximum, the same value from every
+    // host thread (calls for different n may run at once)
+    int optin = 0;
+    cudaFuncAttributes fa;
+    EK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    EK(cudaFuncGetAttributes(&fa, k_sytrd));
+    const int dyn_max = optin - (int)fa.sharedSizeBytes;  // static shared memory counts too
+    if (smem > (size_t)dyn_max) return cudaErrorInvalidValue;
+    EK(cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_max));
     EK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sytrd, kT, smem));
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     // one block per SM (the rows of a step spread over every SM's FP64

@@ -36,15 +36,25 @@ def test_bands_match_oracle_and_published(fits, golden, run, i):
 
 
 def test_solver_paths_agree(fits):
+    """The library's batched solver (default), cuSOLVER's batched routine and
+    cuSOLVER one matrix per call give the same bands and the same gradient."""
     c = fits["w_cdse"].crystals[0]
     bc = bulk.BulkCrystal(c)
     p = bc.type_params(fb.best_atom_params("w_cdse")[0])
-    a = bc.bands(p)
-    path = bc.solver_path
+    rng = np.random.default_rng(4)
+    dl = rng.uniform(-1.0, 1.0, (bc.nk, bc.nev))
+    a, ga = bc.backward(p, dl)
+    assert bc.solver_path == 2
+    bc.set_eigensolver("cusolver")
+    b, gb = bc.backward(p, dl)
+    assert bc.solver_path in (0, 1)
     bc.set_solver(False)
-    b = bc.bands(p)
-    assert bc.solver_path == 0 and path in (0, 1)
+    c2 = bc.bands(p)
+    assert bc.solver_path == 0
     assert np.abs(a - b).max() < 1e-9
+    assert np.abs(a - c2).max() < 1e-9
+    # the gradient (eigenvectors, degenerate clusters by perturbation theory)
+    assert np.abs(ga - gb).max() <= 1e-8 * max(1.0, np.abs(gb).max())
     bc.close()
 
 
