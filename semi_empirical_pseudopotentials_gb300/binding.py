@@ -419,7 +419,9 @@ class Context:
         _check(lib().sep_ctx_set_eigensolver(self.h, int(m)))
 
     def set_fusion(self, enable):
-        """Fused xy plane pass for complex64 Newton steps (nx = ny in 64/96/128)."""
+        """Fused two-pass complex64 Newton steps: the xy plane pass for nx = ny in
+        {40, 48, ..., 128}, the sub-plane and zy passes for nx = ny = nz in
+        {160, 192, 256}.  On by default; off: the four line passes."""
         _check(lib().sep_ctx_set_fusion(self.h, 1 if enable else 0))
 
     def set_subspace(self, mode):

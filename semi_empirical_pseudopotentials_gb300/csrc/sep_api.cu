@@ -66,12 +66,14 @@ template <typename T> int upload_grid(sep_ctx* c, GridDev<T>& g) {
     CK(cudaMemcpy(*dst[a], kt.data(), sizeof(T) * kt.size(), cudaMemcpyHostToDevice));
   }
   g.kcap = (T)c->ktab.cap;
-  const int n1 = (c->nx == c->ny && sizeof(T) == sizeof(float)) ? xy_split_n1((int)c->nx) : 0;
-  if (n1 > 0) {  // x and y tables in the plane pass's position order
-    const int L = (int)c->nx, n2 = L / n1;
+  const int n1x = (c->nx == c->ny && sizeof(T) == sizeof(float)) ? xy_split_n1((int)c->nx) : 0;
+  if (n1x > 0) {  // x and y tables in the fused step's position order
+    const int L = (int)c->nx;
+    const int n1s[2] = {n1x, xy_split_y(L)};
     const std::vector<double>* kxy[2] = {&c->ktab.kx, &c->ktab.ky};
     T** dr[2] = {&g.kxr, &g.kyr};
     for (int a = 0; a < 2; ++a) {
+      const int n1 = n1s[a], n2 = L / n1;
       std::vector<T> kt(L);
       for (int p = 0; p < L; ++p) kt[p] = (T)(*kxy[a])[(p / n1) + n2 * (p % n1)];
       CK(cudaMalloc(dr[a], sizeof(T) * L));

@@ -173,18 +173,16 @@ int newton_loop(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K) 
   return kOk;
 }
 
-// Newton loop with two passes per step: z (forward, k^2, inverse), then the
-// xy plane pass (y and x inverse, epilogue, x and y forward).  Same arithmetic
-// per line as the four line passes.
+// Newton loop with two passes per step: z (forward, k^2, inverse; with the
+// y transform's 8-point stage for the sub-plane form), then the xy pass (y and
+// x inverse, epilogue, x and y forward) on planes or sub-planes.  The plane
+// form does the same arithmetic per line as the four line passes.
 template <typename T>
 int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int K) {
   if constexpr (!std::is_same<T, float>::value) {
-    return arg_fail("the xy plane pass is complex64 only");
+    return arg_fail("the fused xy step is complex64 only");
   } else {
     const GridDev<float>& g = c->g32;
-    GridDev<float> gz = g;  // the z pass sees x and y in the plane pass's order
-    gz.kx = g.kxr;
-    gz.ky = g.kyr;
     const long long n = c->n;
     cx<float>* hist = c->w_hist.as<cx<float>>();
     const float* an = c->w_coef.as<float>();
@@ -196,7 +194,7 @@ int newton_loop_xy(sep_ctx* c, int Bc, long long nstates, long ms, long nc, int 
     io.src = nullptr;
     io.coefs = c->w_steps.as<float>();
     for (long j = 1; j < nc; ++j) {
-      CK(run_pass<float>(2, kFwdKInv, gz, io, Bc, s));
+      CK(run_xy_zpass(g, io, Bc, s));
       io.psi_in = hist + (long long)((j - 1) % K) * Bc * n;
       io.psi_out = hist + (long long)(j % K) * Bc * n;
       io.step = (int)j;

@@ -270,5 +270,8 @@ template <int S, typename T> struct Dft<10, S, T> : DftPQ<2, 5, S, T> {};
 template <int S, typename T> struct Dft<12, S, T> : DftPQ<3, 4, S, T> {};
 template <int S, typename T> struct Dft<14, S, T> : DftPQ<2, 7, S, T> {};
 template <int S, typename T> struct Dft<16, S, T> : DftPQ<4, 4, S, T> {};
+template <int S, typename T> struct Dft<20, S, T> : DftPQ<4, 5, S, T> {};
+template <int S, typename T> struct Dft<24, S, T> : DftPQ<8, 3, S, T> {};
+template <int S, typename T> struct Dft<32, S, T> : DftPQ<4, 8, S, T> {};
 
 }  // namespace sep

@@ -26,8 +26,8 @@ template <typename T> struct GridDev {
   T kcap = 0;
   T* pot = nullptr;
   int variant[5] = {0, 0, 0, 0, 0};  // tile shape per pass kind (autotuned)
-  // k^2 axis tables in the xy plane pass's digit-reversed position order
-  // (complex64 grids with nx = ny in {64, 96, 128}; else null)
+  // k^2 axis tables of x and y in the fused step's digit-reversed position
+  // order (complex64 grids with a fused step; else null)
   T* kxr = nullptr;
   T* kyr = nullptr;
 };
@@ -62,16 +62,28 @@ template <typename T>
 cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& io, int B,
                      cudaStream_t s);
 
-// Fused xy plane pass of a complex64 Newton step (sep_xypass.cuh): modes kFwd,
-// kInvEpi, kInvEpiFwd on whole z-planes; for nx = ny in {64, 96, 128}.
-// Between xy plane passes x and y are kept in digit-reversed position order:
-// element k = k2 + N2 k1 of an axis of length L = N1 N2 at position k1 + N1 k2,
-// N1 = xy_split_n1(L) (0: no plane pass for L).
+// Fused two-pass Newton step of complex64 grids with nx = ny: the xy pass
+// (modes kFwd, kInvEpi, kInvEpiFwd) and the z pass of that step.  For nx in
+// {40, ..., 128} the xy pass works on whole z-planes (sep_xypass.cuh) and the
+// z pass is the z line pass; for nx = ny = nz in {160, 192, 256} the xy pass
+// works on sub-planes and the z pass also does the y transform's 8-point
+// stage (sep_subplane.cuh).  Between the two passes x and y are kept in
+// digit-reversed position order: element k = k2 + N2 k1 of an axis of length
+// L = N1 N2 at position k1 + N1 k2, N1 = xy_split_n1(L) for x and
+// xy_split_y(L) for y (0: no fused step for L).
 int xy_split_n1(int L);
+int xy_split_y(int L);
 bool xy_supported(const GridDev<float>& g);
 cudaError_t xy_prepare(const GridDev<float>& g);  // before any stream capture
 cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& io, int B,
                         cudaStream_t s);
+cudaError_t run_xy_zpass(const GridDev<float>& g, const PassIO<float>& io, int B,
+                         cudaStream_t s);
+// the sub-plane form (sep_sp_f32.cu)
+bool subplane_length(int L);
+cudaError_t subplane_prepare(int L);
+cudaError_t subplane_launch(int mode, const PassArgs<float>& a, int B, cudaStream_t s);
+cudaError_t zy_launch(const GridDev<float>& g, cx<float>* data, int B, cudaStream_t s);
 
 // out = alpha (T x + V y) + beta y for B complex grids; y may be null (out = alpha T x).
 // scratch: B * n complex; out may not alias x.

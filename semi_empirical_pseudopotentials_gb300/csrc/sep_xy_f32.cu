@@ -1,4 +1,6 @@
-// sep_xy_f32.cu -- launch of the fused xy plane pass (complex64).
+// sep_xy_f32.cu -- launch of the fused xy plane pass (complex64) and dispatch
+// of the fused Newton step's two passes (plane form here, sub-plane form in
+// sep_sp_f32.cu).
 #include "sep_engine.cuh"
 #include "sep_xypass.cuh"
 
@@ -64,11 +66,28 @@ int xy_split_n1(int L) {
   if (L == LL) return Split<LL>::n1;
   SEP_XY_LENGTHS(SEP_XY_N1)
 #undef SEP_XY_N1
+  if (L == 160) return Split<160>::n1;
+  if (L == 192) return Split<192>::n1;
+  if (L == 256) return Split<256>::n1;
   return 0;
 }
 
+// y is split 8 x (L / 8) by both forms (the plane lengths have N1 = 8)
+int xy_split_y(int L) { return xy_split_n1(L) > 0 ? 8 : 0; }
+
+namespace {
+bool plane_length(int L) {
+#define SEP_XY_IS(LL) \
+  if (L == LL) return true;
+  SEP_XY_LENGTHS(SEP_XY_IS)
+#undef SEP_XY_IS
+  return false;
+}
+}  // namespace
+
 bool xy_supported(const GridDev<float>& g) {
-  return g.nx == g.ny && xy_split_n1(g.nx) > 0 && g.kxr && g.kyr;
+  if (g.nx != g.ny || !g.kxr || !g.kyr) return false;
+  return plane_length(g.nx) || (subplane_length(g.nx) && g.nz == g.nx);
 }
 
 cudaError_t xy_prepare(const GridDev<float>& g) {
@@ -76,6 +95,7 @@ cudaError_t xy_prepare(const GridDev<float>& g) {
   if (g.nx == LL) return prepare_len<LL>();
   SEP_XY_LENGTHS(SEP_XY_PREP)
 #undef SEP_XY_PREP
+  if (subplane_length(g.nx)) return subplane_prepare(g.nx);
   return cudaErrorInvalidValue;
 }
 
@@ -99,6 +119,21 @@ cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& 
   if (g.nx == LL) return launch_mode<LL>(mode, a, B, s);
   SEP_XY_LENGTHS(SEP_XY_RUN)
 #undef SEP_XY_RUN
+  if (subplane_length(g.nx)) return subplane_launch(mode, a, B, s);
+  return cudaErrorInvalidValue;
+}
+
+// the z pass of the fused step: the z line pass with x and y looked up in
+// position order, or (sub-plane form) the zy pass
+cudaError_t run_xy_zpass(const GridDev<float>& g, const PassIO<float>& io, int B,
+                         cudaStream_t s) {
+  if (plane_length(g.nx)) {
+    GridDev<float> gz = g;
+    gz.kx = g.kxr;
+    gz.ky = g.kyr;
+    return run_pass<float>(2, kFwdKInv, gz, io, B, s);
+  }
+  if (subplane_length(g.nx)) return zy_launch(g, io.data, B, s);
   return cudaErrorInvalidValue;
 }
 
