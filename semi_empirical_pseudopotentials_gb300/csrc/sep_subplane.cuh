@@ -57,19 +57,21 @@ template <int L, int NT> struct SpShape {
   static constexpr size_t smem_bytes = ((size_t)rows * rs + L) * sizeof(cx<float>);
 };
 
-// zy pass shape per length: TX adjacent columns per brick, threads per block.
-// A thread holds a 64-element block (about 160 registers); the brick is
-// LZ x 8 TX elements (33 to 131 KB).  Fastest measured (zy pass on 0.5 GB of
-// grids, fraction of the copy bandwidth): 160^3 TX 4 0.48, 192^3 TX 4 0.49,
-// 256^3 TX 8 0.40.
+// zy pass shape per length: TX adjacent columns per brick, threads per block,
+// blocks per SM.  A thread holds a 64-element block (about 160 registers); the
+// brick is LZ x 8 TX elements (33 to 131 KB).  Fastest measured (zy pass on
+// 0.5 GB of grids, fraction of the copy bandwidth): 160^3 TX 4 0.48, 192^3
+// TX 4 0.51, 256^3 TX 8 0.40.  The pass is issue-bound (about 60 FP32
+// instructions per element for the two 8-point y stages and the z transform
+// pair) with 12 warps per SM.
 template <int L> struct ZyTune {
-  static constexpr int tx = 8, nt = 128;
+  static constexpr int tx = 8, nt = 128, min_blocks = 1;
 };
 template <> struct ZyTune<160> {
-  static constexpr int tx = 4, nt = 128;
+  static constexpr int tx = 4, nt = 128, min_blocks = 1;
 };
 template <> struct ZyTune<192> {
-  static constexpr int tx = 4, nt = 128;
+  static constexpr int tx = 4, nt = 128, min_blocks = 3;
 };
 
 template <int L, int LZ, int TX> struct ZyShape {
@@ -84,9 +86,10 @@ template <int L, int LZ, int TX> struct ZyShape {
   // half-warp on 16 / TX adjacent p and TX columns (same row) hit 16
   // different bank pairs; 16 adjacent lines of one p stay a permutation of
   // one 16-element group.
+  static constexpr int zg = TX >= 16 ? 1 : 16 / TX;  // period of the swizzle in p
+  static_assert(m % zg == 0, "positions x1 + m k2 share the swizzle of x1");
   static __device__ __forceinline__ int at(int p, int line) {
-    if constexpr (TX >= 16) return p * nl + line;
-    else return p * nl + (line ^ ((p % (16 / TX)) * TX));
+    return p * nl + (line ^ ((p % zg) * TX));
   }
 };
 
@@ -147,7 +150,7 @@ __device__ __forceinline__ void col_fwd_a_to(const C* pl, const C* tw, int x1,
     for (int x2 = 0; x2 < S::n2y; ++x2) v[x2] = pl[x2 * S::rs + col];
     Dft<S::n2y, -1, float>::run(v);
 #pragma unroll
-    for (int k2 = 1; k2 < S::n2y; ++k2) v[k2] = mul<float>(v[k2], tw[(x1 * k2) % L]);
+    for (int k2 = 1; k2 < S::n2y; ++k2) v[k2] = mul<float>(v[k2], tw[x1 * k2]);
 #pragma unroll
     for (int k2 = 0; k2 < S::n2y; ++k2) g[(long long)(S::n1y * k2) * L + col] = v[k2];
   }
@@ -172,7 +175,7 @@ __device__ __forceinline__ void col_fwd_a_inv_a_next(C* pl, const C* tw, int x1,
     for (int x2 = 0; x2 < S::n2y; ++x2) v[x2] = pl[x2 * S::rs + col];
     Dft<S::n2y, -1, float>::run(v);
 #pragma unroll
-    for (int k2 = 1; k2 < S::n2y; ++k2) v[k2] = mul<float>(v[k2], tw[(x1 * k2) % L]);
+    for (int k2 = 1; k2 < S::n2y; ++k2) v[k2] = mul<float>(v[k2], tw[x1 * k2]);
 #pragma unroll
     for (int k2 = 0; k2 < S::n2y; ++k2) gcur[(long long)(S::n1y * k2) * L + col] = v[k2];
     Dft<S::n2y, +1, float>::run(u);
@@ -193,7 +196,7 @@ template <int L, int NT> __device__ __forceinline__ void row_inv_b(C* pl, const 
     for (int k1 = 0; k1 < S::n1; ++k1) v[k1] = p[k1];
     Dft<S::n1, +1, float>::run(v);
 #pragma unroll
-    for (int n1 = 1; n1 < S::n1; ++n1) v[n1] = mulc<float>(v[n1], tw[(n1 * k2) % L]);
+    for (int n1 = 1; n1 < S::n1; ++n1) v[n1] = mulc<float>(v[n1], tw[n1 * k2]);
 #pragma unroll
     for (int n1 = 0; n1 < S::n1; ++n1) p[n1] = v[n1];
   }
@@ -257,7 +260,7 @@ __device__ __forceinline__ void row_inv_a_epi(C* pl, const C* tw, const PassArgs
     if constexpr (FWD) {
       Dft<S::n2, -1, float>::run(u);
 #pragma unroll
-      for (int k2 = 1; k2 < S::n2; ++k2) u[k2] = mul<float>(u[k2], tw[(n1 * k2) % L]);
+      for (int k2 = 1; k2 < S::n2; ++k2) u[k2] = mul<float>(u[k2], tw[n1 * k2]);
 #pragma unroll
       for (int k2 = 0; k2 < S::n2; ++k2) p[S::n1 * k2] = u[k2];
     }
@@ -278,7 +281,7 @@ __device__ __forceinline__ void row_fwd_a_from(C* pl, const C* tw, int y1,
     for (int x2 = 0; x2 < S::n2; ++x2) v[x2] = q[S::n1 * x2];
     Dft<S::n2, -1, float>::run(v);
 #pragma unroll
-    for (int k2 = 1; k2 < S::n2; ++k2) v[k2] = mul<float>(v[k2], tw[(x1 * k2) % L]);
+    for (int k2 = 1; k2 < S::n2; ++k2) v[k2] = mul<float>(v[k2], tw[x1 * k2]);
     C* p = pl + row * S::rs + x1;
 #pragma unroll
     for (int k2 = 0; k2 < S::n2; ++k2) p[S::n1 * k2] = v[k2];
@@ -372,8 +375,9 @@ __global__ void __launch_bounds__(NT, MINB) subplane_pass(PassArgs<float> a, int
 
 // One block per brick (TX columns x0.., the 8 position rows 8 k2y.., all z,
 // grid b) = (blockIdx.x, blockIdx.y, blockIdx.z).  z = x1 + M x2 (M = LZ / 8).
-template <int L, int LZ, int TX = ZyTune<L>::tx, int NT = ZyTune<L>::nt>
-__global__ void __launch_bounds__(NT) zy_pass(ZyArgs a) {
+template <int L, int LZ, int TX = ZyTune<L>::tx, int NT = ZyTune<L>::nt,
+          int MINB = ZyTune<L>::min_blocks>
+__global__ void __launch_bounds__(NT, MINB) zy_pass(ZyArgs a) {
   using C = cx<float>;
   using S = ZyShape<L, LZ, TX>;
   constexpr int M = S::m, NL = S::nl;
@@ -413,16 +417,22 @@ __global__ void __launch_bounds__(NT) zy_pass(ZyArgs a) {
 #pragma unroll
       for (int k1 = 0; k1 < 8; ++k1) v[k1][x2] = c[k1];
     }
-    C t[8];  // the item's twiddles, read once (the brick stores could alias them)
+    // the item's twiddles (x1 k2 < LZ), read once: the brick stores could alias them
+    C t[8];
 #pragma unroll
-    for (int k2 = 1; k2 < 8; ++k2) t[k2] = tz[(x1 * k2) % LZ];
+    for (int k2 = 1; k2 < 8; ++k2) t[k2] = tz[x1 * k2];
+    // brick (x1 + M k2, k1 TX + x) = q[M NL k2 + (k1 ^ sw) TX]: every position
+    // of the item has the swizzle of x1
+    C* q = br + x1 * NL + x;
+    const int sw = x1 % S::zg;
 #pragma unroll
     for (int k1 = 0; k1 < 8; ++k1) {
       Dft<8, -1, float>::run(v[k1]);
 #pragma unroll
       for (int k2 = 1; k2 < 8; ++k2) v[k1][k2] = mul<float>(v[k1][k2], t[k2]);
+      C* qk = q + (k1 ^ sw) * TX;
 #pragma unroll
-      for (int k2 = 0; k2 < 8; ++k2) br[S::at(x1 + M * k2, k1 * TX + x)] = v[k1][k2];
+      for (int k2 = 0; k2 < 8; ++k2) qk[k2 * (M * NL)] = v[k1][k2];
     }
   }
   __syncthreads();
@@ -431,9 +441,13 @@ __global__ void __launch_bounds__(NT) zy_pass(ZyArgs a) {
   // conjugate twiddle): item (line, k2)
   for (int i = tid; i < NL * 8; i += NT) {
     const int line = i % NL, k2 = i / NL;
+    C* q = br + k2 * (M * NL);
+    int ls[S::zg];  // the line's swizzled index for each residue of x1
+#pragma unroll
+    for (int j = 0; j < S::zg; ++j) ls[j] = line ^ (j * TX);
     C w[M];
 #pragma unroll
-    for (int x1 = 0; x1 < M; ++x1) w[x1] = br[S::at(x1 + M * k2, line)];
+    for (int x1 = 0; x1 < M; ++x1) w[x1] = q[x1 * NL + ls[x1 % S::zg]];
     Dft<M, -1, float>::run(w);
     const float kxy = a.kx[x0 + line % TX] + a.ky[y0 + line / TX];
 #pragma unroll
@@ -444,24 +458,27 @@ __global__ void __launch_bounds__(NT) zy_pass(ZyArgs a) {
     }
     Dft<M, +1, float>::run(w);
 #pragma unroll
-    for (int n1 = 1; n1 < M; ++n1) w[n1] = mulc<float>(w[n1], tz[(n1 * k2) % LZ]);
+    for (int n1 = 1; n1 < M; ++n1) w[n1] = mulc<float>(w[n1], tz[n1 * k2]);  // n1 k2 < LZ
 #pragma unroll
-    for (int n1 = 0; n1 < M; ++n1) br[S::at(n1 + M * k2, line)] = w[n1];
+    for (int n1 = 0; n1 < M; ++n1) q[n1 * NL + ls[n1 % S::zg]] = w[n1];
   }
   __syncthreads();
   // item (x, n1): z inverse stage A' (inverse DFT_8 over k2 per row: natural
   // z = n1 + M n2), then y inverse stage B' (inverse DFT_8 over the rows,
   // conjugate twiddle w_L^(ny k2y)) -> rows y0 + ny
-  C t[8];  // the brick's y twiddles
+  C t[8];  // the brick's y twiddles (ny k2y < L)
 #pragma unroll
-  for (int ny = 1; ny < 8; ++ny) t[ny] = ty[(ny * k2y) % L];
+  for (int ny = 1; ny < 8; ++ny) t[ny] = ty[ny * k2y];
   for (int i = tid; i < TX * M; i += NT) {
     const int x = i % TX, n1 = i / TX;
+    const C* q = br + n1 * NL + x;
+    const int sw = n1 % S::zg;
     C u[8][8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
+      const C* qr = q + (r ^ sw) * TX;
 #pragma unroll
-      for (int k2 = 0; k2 < 8; ++k2) u[r][k2] = br[S::at(n1 + M * k2, r * TX + x)];
+      for (int k2 = 0; k2 < 8; ++k2) u[r][k2] = qr[k2 * (M * NL)];
       Dft<8, +1, float>::run(u[r]);
     }
     C* p = g + (long long)n1 * zs + x;
