@@ -256,13 +256,28 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     c->xy_ready = true;
   }
   // chunks of pairs [first, first + count): at most Bc each.  With host
-  // buffers the last chunk is halved while it has 8 pairs or more (32 pairs:
-  // 16, 8, 4, 4), so that each chunk's output copy runs under the next
-  // chunk's filter even when the host copies are slow, and only the last
-  // few pairs' copy is not overlapped
+  // buffers each chunk's output copy runs under the next chunk's filter, and
+  // only the last chunk's copy is not overlapped; small chunks filter fewer
+  // pairs per second (on a 128^3 grid 4 pairs cost 17% more per pair than
+  // 32).  So the last chunk splits off a tail:
+  //  - copy/filter ratio r measured by an earlier call: the smallest tail t
+  //    (at least 4 pairs) whose filter time covers the copy of the rest,
+  //    r (c - t) <= t (32 pairs at r = 0.06: 28 + 4);
+  //  - not measured yet: halved while it has 8 pairs or more (32 pairs:
+  //    16, 8, 4, 4), which overlaps the copies even when they are slow.
   std::vector<std::pair<long long, long long>> chunks;
   for (long long b0 = 0; b0 < B; b0 += Bc) chunks.push_back({b0, std::min<long long>(Bc, B - b0)});
-  if (host) {
+  if (host && c->host_copy_ratio >= 0.0) {
+    auto& last = chunks.back();
+    if (last.second >= 8) {
+      const double r = c->host_copy_ratio;
+      long long t = (long long)std::ceil(r * (double)last.second / (1.0 + r));
+      t = std::max<long long>(t, 4);
+      t = std::min<long long>(t, last.second / 2);
+      last.second -= t;
+      chunks.push_back({last.first + last.second, t});
+    }
+  } else if (host) {
     while (chunks.back().second >= 8) {
       auto& last = chunks.back();
       const long long second = last.second / 2;
@@ -272,11 +287,14 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
   }
   const long long nchunks = (long long)chunks.size();
   std::vector<cudaEvent_t> ev;  // per chunk: start states up, output computed
+  // timing of chunk 0: filter (on the stream) and output copy (on d2h)
+  cudaEvent_t tm[4] = {nullptr, nullptr, nullptr, nullptr};
   if (host) {
     for (cudaStream_t* st : {&c->h2d, &c->d2h})
       if (!*st) CK(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
     ev.assign(2 * nchunks, nullptr);
     for (auto& e : ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : tm) CK(cudaEventCreate(&e));
   }
   auto chunk_states = [&](long long k, long long& s0, long long& nst) {
     s0 = 2 * chunks[k].first;
@@ -303,6 +321,7 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
         break;
       }
     }
+    if (host && k == 0) CK(cudaEventRecord(tm[0], c->stream));
     CK(pack_pairs<T, double>(d_start + s0 * n, nst, n, c->w_hist.as<cx<T>>(), c->stream));
     if (c->use_graphs) {
       const long long key[8] = {bc, nst, ms, nc, K, (long long)(size_t)c->w_hist.p,
@@ -338,16 +357,25 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     CK(unpack_accumulators<T>(c->w_acc.as<T>(), bc, n, (int)ms, nst, dst, c->stream));
     if (host) {  // the chunk's output goes down while the next chunk is filtered
       CK(cudaEventRecord(ev[2 * k + 1], c->stream));
+      if (k == 0) CK(cudaEventRecord(tm[1], c->stream));
       CK(cudaStreamWaitEvent(c->d2h, ev[2 * k + 1], 0));
+      if (k == 0) CK(cudaEventRecord(tm[2], c->d2h));
       CK(cudaMemcpyAsync(host->out + s0 * ms * n, dst, sizeof(double) * (size_t)(nst * ms * n),
                          cudaMemcpyDeviceToHost, c->d2h));
+      if (k == 0) CK(cudaEventRecord(tm[3], c->d2h));
     }
   }
   if (host) {
     cudaError_t e1 = cudaStreamSynchronize(c->h2d);
     cudaError_t e2 = cudaStreamSynchronize(c->d2h);
     cudaError_t e3 = cudaStreamSynchronize(c->stream);
+    float t_filter = 0.f, t_copy = 0.f;
+    if (rc == kOk && e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess &&
+        cudaEventElapsedTime(&t_filter, tm[0], tm[1]) == cudaSuccess &&
+        cudaEventElapsedTime(&t_copy, tm[2], tm[3]) == cudaSuccess && t_filter > 0.f)
+      c->host_copy_ratio = (double)t_copy / (double)t_filter;
     for (auto e : ev) cudaEventDestroy(e);
+    for (auto e : tm) cudaEventDestroy(e);
     if (rc == kOk) {
       CK(e1);
       CK(e2);

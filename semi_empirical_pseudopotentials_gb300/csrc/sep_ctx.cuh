@@ -64,6 +64,9 @@ struct sep_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t h2d = nullptr, d2h = nullptr;  // host copies beside the filter (sep_filter)
+  // output copy time over filter time per pair, measured on the previous
+  // host-buffer filter call (< 0: not yet measured); sets the chunk plan
+  double host_copy_ratio = -1.0;
   cusolverDnHandle_t solver = nullptr;
   int precision = 0;
   long nx = 0, ny = 0, nz = 0;
