@@ -285,7 +285,7 @@ TRAFFIC_PER_PAIR_128 = {"y_fwd": (201.354752e6 + 142.915584e6) / 12,
 
 def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):
     """Compulsory HBM bytes of one launch (c: bytes per complex, r: per real)."""
-    if kind in ("x_fwd", "y_fwd", "z_fki", "y_inv"):
+    if kind in ("x_fwd", "y_fwd", "z_fki", "y_inv", "xy_z"):
         return 2 * c * n * npairs                      # read + write the grids
     if kind in ("x_inv_epi_fwd", "xy_inv_epi_fwd"):
         return (4 * c) * n * npairs + r * n            # T in/out, psi_in, psi_out, V once
@@ -686,13 +686,18 @@ def run_sep(args):
         peaks = measured_peaks()
         # roofline of the dominant kernel: per-launch device times of each kernel kind
         names = ["x_fwd", "y_fwd", "z_fki", "y_inv", "x_inv_epi_fwd", "accumulate",
-                 "xy_inv_epi_fwd"]
+                 "xy_inv_epi_fwd", "xy_z"]
         npairs = (ns + 1) // 2
-        per = ctx.time_passes(npairs, reps=10)
-        if per[6] > 0:  # fused xy plane pass: z and xy passes per Newton step
-            launches = [0, 0, nc - 1, 0, 0, -(-nc // BLOCK_STEPS), nc]
+        per = list(ctx.time_passes(npairs, reps=10))
+        # the fused step's two passes: on the cubic 128^3 grid the sub-plane
+        # pass (xy_inv_epi_fwd) and the zy pass (xy_z)
+        fused = ctx.time_fused_step(npairs, reps=10)
+        per[6] = fused[0]
+        per.append(fused[1])
+        if per[6] > 0:  # fused step: xy and z passes per Newton step
+            launches = [0, 0, 0, 0, 0, -(-nc // BLOCK_STEPS), nc, nc - 1]
         else:
-            launches = [1, nc - 1, nc - 1, nc - 1, nc - 1, -(-nc // BLOCK_STEPS), 0]
+            launches = [1, nc - 1, nc - 1, nc - 1, nc - 1, -(-nc // BLOCK_STEPS), 0, 0]
         share = [p * l for p, l in zip(per, launches)]
         k = int(np.argmax(share))
         byts = algorithmic_bytes(names[k], npairs, n, 8, 4, kblock=BLOCK_STEPS)
@@ -730,7 +735,7 @@ def run_sep(args):
         per64 = ctx64.time_passes(npairs, reps=3)
         extras["fp64"] = {"value": ns * (ncs - 1) / t64, "unit": "applies/s",
                           "sample": f"{ns} states x {ncs - 1} Newton steps",
-                          "per_launch_ms": dict(zip(names, [round(p, 4) for p in per64])),
+                          "per_launch_ms": dict(zip(names[:7], [round(p, 4) for p in per64])),
                           "note": "complex128 line passes run at the FP64 pipe rate "
                                   "(about 1.25 TFLOP/s on this part)"}
         extras["subspace_gram"] = subspace_gram(sep, ctx, out_d, ns * ms, n, S.dv, peaks)
@@ -807,8 +812,9 @@ def run_sep(args):
             torch.cuda.empty_cache()
 
     if rank == 0:
-        # pack, first forward transform, per Newton step 2 (fused xy plane pass,
-        # nx = ny = 128 in complex64) or 4 line passes, the accumulations, convert
+        # pack, first forward transform, per Newton step 2 (the fused step: the
+        # sub-plane and zy passes on the cubic 128^3 grid) or 4 line passes,
+        # the accumulations, convert
         fused = S.dims[0] == S.dims[1] and S.dims[0] in (40, 48, 56, 64, 72, 80, 96, 112, 128)
         launches_step = 1 + 1 + (2 if fused else 4) * (nc - 1) + -(-nc // BLOCK_STEPS) + 1
         line = {"metric": "Hpsi applies/s at 128^3", "value": value, "unit": "applies/s",

@@ -319,6 +319,13 @@ int sep_eigh_dev(double *a_dev, long n, double *w_dev, double *work_dev, void *c
  * not use it).  No counterpart in the reference; used for the roofline
  * report. */
 int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
+/* The two passes of the fused complex64 Newton step (sep_ctx_set_fusion) on
+ * npairs grids, average device ms per launch over reps launches: ms_out[0]
+ * the xy pass (plane or sub-plane form, with the epilogue and the forward
+ * transforms), ms_out[1] the z pass of that step (the z line pass, or the zy
+ * pass of the sub-plane form).  Both 0 when the context has no fused step.
+ * No counterpart in the reference; used for the roofline report. */
+int sep_time_fused_step(sep_ctx *ctx, long npairs, int reps, double *ms_out);
 
 /* ---- normalisation that allocates nothing ------------------------------
  * filter/norm.c:40-54 (psi_m <- psi_m / sqrt(dv sum_g psi_m(g)^2)) on m real

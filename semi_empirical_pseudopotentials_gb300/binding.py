@@ -81,6 +81,7 @@ def lib():
         L.sep_vbuild_backward.argtypes = [vp, C.c_long, dp, ip, dp, C.c_long, dp, dp, lp,
                                           C.c_long, dp, dp, dp, dp]
         L.sep_time_passes.argtypes = [vp, C.c_long, C.c_int, dp]
+        L.sep_time_fused_step.argtypes = [vp, C.c_long, C.c_int, dp]
         L.sep_hf_density.argtypes = [vp, dp, C.c_long, dp, dp]
         L.sep_ctx_autotune.argtypes = [vp, C.c_long, C.c_int, ip]
         L.sep_batch_create.argtypes = [C.c_int, C.POINTER(vp), lp, C.c_long, C.c_long,
@@ -386,6 +387,14 @@ class Context:
         accumulate, and the fused xy plane pass (0 when it does not apply)."""
         out = np.zeros(7)
         _check(lib().sep_time_passes(self.h, npairs, reps, _p(out)))
+        return out
+
+    def time_fused_step(self, npairs, reps=10):
+        """Average ms per launch of the fused complex64 step's xy pass and z pass
+        (plane form: xy plane pass and z line pass; sub-plane form: sub-plane
+        pass and zy pass); zeros when the context has no fused step."""
+        out = np.zeros(2)
+        _check(lib().sep_time_fused_step(self.h, npairs, reps, _p(out)))
         return out
 
     def vbuild(self, xyz, types, tab_r, tab_v, tab_n, mins, scale=None, install=True):

@@ -69,7 +69,7 @@ template <typename T> int upload_grid(sep_ctx* c, GridDev<T>& g) {
   const int n1x = (c->nx == c->ny && sizeof(T) == sizeof(float)) ? xy_split_n1((int)c->nx) : 0;
   if (n1x > 0) {  // x and y tables in the fused step's position order
     const int L = (int)c->nx;
-    const int n1s[2] = {n1x, xy_split_y(L)};
+    const int n1s[2] = {n1x, xy_split_y(L, (int)c->nz)};
     const std::vector<double>* kxy[2] = {&c->ktab.kx, &c->ktab.ky};
     T** dr[2] = {&g.kxr, &g.kyr};
     for (int a = 0; a < 2; ++a) {
@@ -630,6 +630,12 @@ int sep_time_passes(sep_ctx* c, long npairs, int reps, double* ms_out) {
   RET(check_ctx(c));
   if (!ms_out) return arg_fail("sep_time_passes: null argument");
   return time_passes_device(c, npairs, reps, ms_out);
+}
+
+int sep_time_fused_step(sep_ctx* c, long npairs, int reps, double* ms_out) {
+  RET(check_ctx(c));
+  if (!ms_out) return arg_fail("sep_time_fused_step: null argument");
+  return time_fused_step_device(c, npairs, reps, ms_out);
 }
 
 int sep_ctx_set_refine(sep_ctx* c, int steps) {

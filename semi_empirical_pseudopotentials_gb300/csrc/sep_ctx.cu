@@ -1265,6 +1265,53 @@ int subspace_rotate_device(sep_ctx* c, const double* W, const double* X, long lo
   return oz_check(c);
 }
 
+// the two passes of the fused complex64 Newton step: ms_out[0] the xy pass
+// (plane or sub-plane, step mode), ms_out[1] its z pass (z line pass or zy
+// pass); both 0 when the context has no fused step
+int time_fused_step_device(sep_ctx* c, long npairs, int reps, double* ms_out) {
+  ms_out[0] = ms_out[1] = 0.0;
+  if (npairs < 1 || reps < 1) return arg_fail("sep_time_fused_step: npairs, reps >= 1");
+  if (c->precision != 1 || !use_xy<float>(c)) return kOk;
+  if (!c->xy_ready) {
+    CK(xy_prepare(c->g32));
+    c->xy_ready = true;
+  }
+  const long long n = c->n;
+  RET(grow(c, c->w_hist, sizeof(cx<float>) * (size_t)n * 2 * npairs));
+  RET(grow(c, c->w_fft, sizeof(cx<float>) * (size_t)n * npairs));
+  CK(cudaMemsetAsync(c->w_hist.p, 0, c->w_hist.bytes, c->stream));
+  CK(cudaMemsetAsync(c->w_fft.p, 0, c->w_fft.bytes, c->stream));
+  cx<float>* hist = c->w_hist.as<cx<float>>();
+  PassIO<float> io;
+  io.data = c->w_fft.as<cx<float>>();
+  io.psi_in = hist;
+  io.psi_out = hist + (long long)n * npairs;
+  io.alpha = 0.1f;
+  io.beta = -0.5f;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int rc = kOk;
+  for (int k = 0; k < 2 && rc == kOk; ++k) {
+    for (int r = -1; r < reps && rc == kOk; ++r) {  // r = -1: warm-up
+      if (r == 0 && cudaEventRecord(e0, c->stream) != cudaSuccess) rc = arg_fail("event");
+      const cudaError_t e = k == 0 ? run_xy_pass(kInvEpiFwd, c->g32, io, (int)npairs, c->stream)
+                                   : run_xy_zpass(c->g32, io, (int)npairs, c->stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "fused step pass", __LINE__);
+    }
+    float t = 0.f;
+    if (rc == kOk) {
+      CK(cudaEventRecord(e1, c->stream));
+      CK(cudaEventSynchronize(e1));
+      CK(cudaEventElapsedTime(&t, e0, e1));
+      ms_out[k] = (double)t / reps;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out) {
   if (npairs < 1 || reps < 1 || c->block_steps < 2)
     return arg_fail("sep_time_passes: npairs, reps >= 1 and block steps >= 2");

@@ -149,6 +149,7 @@ int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,
 // also: rows scaled by the same factors as psi's (H psi follows psi)
 int normalize_device(sep_ctx* c, double* d_psi, long m, double* also = nullptr);
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out);
+int time_fused_step_device(sep_ctx* c, long npairs, int reps, double* ms_out);
 int subspace_gemm_device(sep_ctx* c, const double* A, const double* B, long long m, long long n,
                          long long k, double alpha, bool sym, double* C);
 int subspace_rotate_device(sep_ctx* c, const double* W, const double* X, long long m,

@@ -63,16 +63,17 @@ cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& i
                      cudaStream_t s);
 
 // Fused two-pass Newton step of complex64 grids with nx = ny: the xy pass
-// (modes kFwd, kInvEpi, kInvEpiFwd) and the z pass of that step.  For nx in
-// {40, ..., 128} the xy pass works on whole z-planes (sep_xypass.cuh) and the
-// z pass is the z line pass; for nx = ny = nz in {160, 192, 256} the xy pass
-// works on sub-planes and the z pass also does the y transform's 8-point
-// stage (sep_subplane.cuh).  Between the two passes x and y are kept in
-// digit-reversed position order: element k = k2 + N2 k1 of an axis of length
-// L = N1 N2 at position k1 + N1 k2, N1 = xy_split_n1(L) for x and
-// xy_split_y(L) for y (0: no fused step for L).
+// (modes kFwd, kInvEpi, kInvEpiFwd) and the z pass of that step.  Cubic grids
+// with nx in {128, 160, 192, 256} take the sub-plane form: the xy pass works
+// on sub-planes and the z pass also does the y transform's R-point stage
+// (sep_subplane.cuh).  Other grids with nx in {40, ..., 128} take the plane
+// form: the xy pass works on whole z-planes (sep_xypass.cuh) and the z pass is
+// the z line pass.  Between the two passes x and y are kept in digit-reversed
+// position order: element k = k2 + N2 k1 of an axis of length L = N1 N2 at
+// position k1 + N1 k2, N1 = xy_split_n1(nx) for x and xy_split_y(nx, nz) for
+// y (0: no fused step).
 int xy_split_n1(int L);
-int xy_split_y(int L);
+int xy_split_y(int nx, int nz);
 bool xy_supported(const GridDev<float>& g);
 cudaError_t xy_prepare(const GridDev<float>& g);  // before any stream capture
 cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& io, int B,
@@ -81,6 +82,7 @@ cudaError_t run_xy_zpass(const GridDev<float>& g, const PassIO<float>& io, int B
                          cudaStream_t s);
 // the sub-plane form (sep_sp_f32.cu)
 bool subplane_length(int L);
+int subplane_rows(int L);  // R
 cudaError_t subplane_prepare(int L);
 cudaError_t subplane_launch(int mode, const PassArgs<float>& a, int B, cudaStream_t s);
 cudaError_t zy_launch(const GridDev<float>& g, cx<float>* data, int B, cudaStream_t s);

@@ -1,5 +1,5 @@
 // sep_sp_f32.cu -- launch of the sub-plane pass and the zy pass (complex64),
-// the fused Newton step for nx = ny = nz in {160, 192, 256}.
+// the fused Newton step for nx = ny = nz in {128, 160, 192, 256}.
 #include "sep_engine.cuh"
 #include "sep_subplane.cuh"
 
@@ -36,7 +36,7 @@ template <int L> cudaError_t launch_zy(const ZyArgs& z, int B, cudaStream_t s) {
   using T = ZyTune<L>;
   using S = ZyShape<L, L, T::tx>;
   if (B < 1 || B > 65535) return cudaErrorInvalidValue;
-  const dim3 grid(L / T::tx, L / 8, (unsigned)B);
+  const dim3 grid(L / T::tx, L / S::r, (unsigned)B);
   zy_pass<L, L><<<grid, T::nt, S::smem_bytes, s>>>(z);
   return cudaGetLastError();
 }
@@ -67,7 +67,7 @@ cudaError_t launch_sp_mode(int mode, const PassArgs<float>& a, int B, cudaStream
 
 }  // namespace
 
-#define SEP_SP_LENGTHS(X) X(160) X(192) X(256)
+#define SEP_SP_LENGTHS(X) X(128) X(160) X(192) X(256)
 
 bool subplane_length(int L) {
 #define SEP_SP_IS(LL) \
@@ -75,6 +75,14 @@ bool subplane_length(int L) {
   SEP_SP_LENGTHS(SEP_SP_IS)
 #undef SEP_SP_IS
   return false;
+}
+
+int subplane_rows(int L) {
+#define SEP_SP_R(LL) \
+  if (L == LL) return SpRows<LL>::r;
+  SEP_SP_LENGTHS(SEP_SP_R)
+#undef SEP_SP_R
+  return 0;
 }
 
 cudaError_t subplane_prepare(int L) {

@@ -1,27 +1,29 @@
-// sep_subplane.cuh -- the two-pass complex64 Newton step for xy planes that
-// do not fit in one block's shared memory (nx = ny = L in {160, 192, 256}; a
-// 192^2 plane is 295 KB).
+// sep_subplane.cuh -- the two-pass complex64 Newton step on sub-planes, for
+// cubic grids L^3 with L in {128, 160, 192, 256}: xy planes that do not fit
+// in one block's shared memory (a 192^2 plane is 295 KB), and 128^2 planes,
+// which fit only one per SM.
 //
 // Each 1-D transform is a four-step split (sep_fftpass.cuh): for a length
 // L = N1 N2, forward stage A (per residue x1: DFT_N2 over x1 + N1 x2,
 // twiddle w_L^(x1 k2)) and stage B (per k2: DFT_N1 over x1 + N1 k2, element
 // k2 + N2 k1 left at position k1 + N1 k2); inverse stage B' then A'.  Here y
-// is split 8 x (L / 8) and z (LZ / 8) x 8.  Stage A of y only couples the
-// L / 8 rows of one residue, and stage B only 8 adjacent rows, so:
+// is split R x (L / R) (R = 4 for 128, 8 for 160, 192, 256) and z
+// (LZ / 8) x 8.  Stage A of y only couples the L / R rows of one residue, and
+// stage B only R adjacent rows, so:
 //
-//   zy pass (bricks of 8 adjacent position rows x TX columns x all z):
+//   zy pass (bricks of R adjacent position rows x TX columns x all z):
 //     y stage B, z forward, k^2 (filter/init.c:141-142), z inverse,
 //     y stage B'  -- the k^2 multiply sees the full (kx, ky, kz) spectrum
-//   sub-plane pass (units (grid, z, residue y1): the L / 8 rows y1 + 8 j):
+//   sub-plane pass (units (grid, z, residue y1): the L / R rows y1 + R j):
 //     y stage A', x inverse, psi_j = alpha (T + V psi_{j-1}) + beta psi_{j-1}
 //     (filter/hnorm.c:11-39), x forward, y stage A
 //
 // which is two passes over the grids per Newton step where the line passes
-// take four.  A thread of the zy pass holds an 8 x 8 block (8 rows, the 8 z
-// of one residue x1 + (LZ / 8) x2): it does the y DFT_8s and the z stage-A
+// take four.  A thread of the zy pass holds an R x 8 block (R rows, the 8 z
+// of one residue x1 + (LZ / 8) x2): it does the y DFT_Rs and the z stage-A
 // DFT_8s of the block in registers, so a brick crosses shared memory twice,
 // as a z line pass does.  The sub-plane pass keeps x in the line passes'
-// split (N1 x 16) and its 16-, 20-, 24- or 32-row sub-planes (17 to 66 KB) in
+// split (N1 x 16) and its 20-, 24- or 32-row sub-planes (26 to 66 KB) in
 // shared memory, several blocks per SM.  Between passes x and y are kept in
 // digit-reversed position order (element k2 + N2 k1 of an axis at position
 // k1 + N1 k2), z in natural order; the k^2 tables follow the same order.
@@ -31,25 +33,42 @@
 
 namespace sep {
 
-// sub-plane pass launch shape per length: threads per block, blocks per SM
-// (fastest measured, step pass on 0.5 GB of grids, fraction of the copy
-// bandwidth: 160^2 0.75, 192^2 0.84, 256^2 0.75)
+// sub-plane pass launch shape per length: threads per block, blocks per SM,
+// whether the last stage of a unit runs with the first of the next (fastest
+// measured, step pass on 0.5 GB of grids, fraction of the copy bandwidth:
+// 128^2 0.84, 160^2 0.75, 192^2 0.84, 256^2 0.75)
 template <int L> struct SpTune {
   static constexpr int nt = 128, min_blocks = 4;
+  static constexpr bool fuse_next = true;
+};
+template <> struct SpTune<128> {  // 32-row sub-planes: the fused column stage spills
+  static constexpr int nt = 128, min_blocks = 4;
+  static constexpr bool fuse_next = false;
 };
 template <> struct SpTune<160> {
   static constexpr int nt = 64, min_blocks = 6;
+  static constexpr bool fuse_next = true;
 };
 template <> struct SpTune<192> {
   static constexpr int nt = 96, min_blocks = 4;
+  static constexpr bool fuse_next = true;
 };
 template <> struct SpTune<256> {
   static constexpr int nt = 128, min_blocks = 3;
+  static constexpr bool fuse_next = true;
+};
+
+// R: the y transform's stage-B radix, done by the zy pass
+template <int L> struct SpRows {
+  static constexpr int r = 8;
+};
+template <> struct SpRows<128> {
+  static constexpr int r = 4;
 };
 
 template <int L, int NT> struct SpShape {
   static constexpr int n1 = Split<L>::n1, n2 = Split<L>::n2;  // x
-  static constexpr int n1y = 8, n2y = L / 8;                   // y
+  static constexpr int n1y = SpRows<L>::r, n2y = L / n1y;      // y
   static constexpr int rows = n2y;  // rows of a sub-plane
   static constexpr int rs = L + 1;  // row stride (elements): rows 2 banks apart
   static constexpr int nt = NT;
@@ -60,10 +79,11 @@ template <int L, int NT> struct SpShape {
 // zy pass shape per length: TX adjacent columns per brick, threads per block,
 // blocks per SM.  A thread holds a 64-element block (about 160 registers); the
 // brick is LZ x 8 TX elements (33 to 131 KB).  Fastest measured (zy pass on
-// 0.5 GB of grids, fraction of the copy bandwidth): 160^3 TX 4 0.48, 192^3
-// TX 4 0.51, 256^3 TX 8 0.40.  The pass is issue-bound (about 60 FP32
-// instructions per element for the two 8-point y stages and the z transform
-// pair) with 12 warps per SM.
+// 0.5 GB of grids, fraction of the copy bandwidth): 128^3 (R = 4) TX 8 0.74,
+// 160^3 TX 4 0.48, 192^3 TX 4 0.51, 256^3 TX 8 0.40.  With R = 8 the pass is
+// issue-bound (about 60 FP32 instructions per element for the two 8-point y
+// stages and the z transform pair) with 12 warps per SM; R = 4 needs about
+// 90 registers and no multiplies in its y stages.
 template <int L> struct ZyTune {
   static constexpr int tx = 8, nt = 128, min_blocks = 1;
 };
@@ -75,8 +95,9 @@ template <> struct ZyTune<192> {
 };
 
 template <int L, int LZ, int TX> struct ZyShape {
-  static constexpr int m = LZ / 8;  // z = x1 + m x2
-  static constexpr int nl = 8 * TX;  // z lines of a brick
+  static constexpr int r = SpRows<L>::r;  // position rows of a brick
+  static constexpr int m = LZ / 8;        // z = x1 + m x2
+  static constexpr int nl = r * TX;       // z lines of a brick
   static_assert(LZ % 8 == 0 && L % 8 == 0 && L % TX == 0, "brick shapes");
   static_assert(nl % 16 == 0 && (TX >= 16 || 16 % TX == 0), "brick swizzle");
   static constexpr size_t smem_bytes =
@@ -304,7 +325,8 @@ __device__ __forceinline__ void prefetch_rows(const void* g, int r0, unsigned es
 // Block b walks the units u = b + k gridDim.x of the batch; unit u is
 // (grid u % B, residue y1 = (u / B) % 8, plane z = u / 8 B), so the blocks
 // running at one time share the planes of V.  MODE as xy_plane_pass.
-template <int L, int MODE, int NT = SpTune<L>::nt, int MINB = SpTune<L>::min_blocks>
+template <int L, int MODE, int NT = SpTune<L>::nt, int MINB = SpTune<L>::min_blocks,
+          bool FUSE = SpTune<L>::fuse_next>
 __global__ void __launch_bounds__(NT, MINB) subplane_pass(PassArgs<float> a, int B) {
   using C = cx<float>;
   using S = SpShape<L, NT>;
@@ -359,7 +381,7 @@ __global__ void __launch_bounds__(NT, MINB) subplane_pass(PassArgs<float> a, int
       __syncthreads();
       sp::row_fwd_b<L, NT>(pl);
       __syncthreads();
-      if (MODE == kInvEpiFwd && un < units) {
+      if (FUSE && MODE == kInvEpiFwd && un < units) {
         long long offn, goffn;
         int y1n;
         geometry(un, offn, goffn, y1n);
@@ -373,14 +395,14 @@ __global__ void __launch_bounds__(NT, MINB) subplane_pass(PassArgs<float> a, int
   }
 }
 
-// One block per brick (TX columns x0.., the 8 position rows 8 k2y.., all z,
+// One block per brick (TX columns x0.., the R position rows R k2y.., all z,
 // grid b) = (blockIdx.x, blockIdx.y, blockIdx.z).  z = x1 + M x2 (M = LZ / 8).
 template <int L, int LZ, int TX = ZyTune<L>::tx, int NT = ZyTune<L>::nt,
           int MINB = ZyTune<L>::min_blocks>
 __global__ void __launch_bounds__(NT, MINB) zy_pass(ZyArgs a) {
   using C = cx<float>;
   using S = ZyShape<L, LZ, TX>;
-  constexpr int M = S::m, NL = S::nl;
+  constexpr int M = S::m, NL = S::nl, R = S::r;
   extern __shared__ __align__(16) unsigned char zy_smem[];
   C* br = reinterpret_cast<C*>(zy_smem);
   C* tz = br + LZ * NL;
@@ -392,30 +414,30 @@ __global__ void __launch_bounds__(NT, MINB) zy_pass(ZyArgs a) {
     kz[m] = a.kz[m];
   }
   for (int m = tid; m < L; m += NT) ty[m] = a.tw_y[m];
-  const int x0 = blockIdx.x * TX, k2y = blockIdx.y, y0 = 8 * k2y;
+  const int x0 = blockIdx.x * TX, k2y = blockIdx.y, y0 = R * k2y;
   const long long zs = (long long)L * L;
   C* __restrict__ g = a.data + (long long)blockIdx.z * zs * LZ + (long long)y0 * L + x0;
   __syncthreads();  // tables
 
-  // item (x, x1): the 8 rows x the 8 z = x1 + M x2 of column x.  y stage B
-  // (DFT_8 over the rows: element k2y + (L / 8) k1 at row y0 + k1), then z
+  // item (x, x1): the R rows x the 8 z = x1 + M x2 of column x.  y stage B
+  // (DFT_R over the rows: element k2y + (L / R) k1 at row y0 + k1), then z
   // stage A (DFT_8 over x2, twiddle w_LZ^(x1 k2)) -> brick (x1 + M k2, k1 TX + x)
   for (int i = tid; i < TX * M; i += NT) {
     const int x = i % TX, x1 = i / TX;
-    C v[8][8];
+    C v[R][8];
     const C* p = g + (long long)x1 * zs + x;
 #pragma unroll
     for (int x2 = 0; x2 < 8; ++x2)
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r][x2] = p[(long long)(M * x2) * zs + (long long)r * L];
+      for (int r = 0; r < R; ++r) v[r][x2] = p[(long long)(M * x2) * zs + (long long)r * L];
 #pragma unroll
     for (int x2 = 0; x2 < 8; ++x2) {
-      C c[8];
+      C c[R];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) c[r] = v[r][x2];
-      Dft<8, -1, float>::run(c);
+      for (int r = 0; r < R; ++r) c[r] = v[r][x2];
+      Dft<R, -1, float>::run(c);
 #pragma unroll
-      for (int k1 = 0; k1 < 8; ++k1) v[k1][x2] = c[k1];
+      for (int k1 = 0; k1 < R; ++k1) v[k1][x2] = c[k1];
     }
     // the item's twiddles (x1 k2 < LZ), read once: the brick stores could alias them
     C t[8];
@@ -426,7 +448,7 @@ __global__ void __launch_bounds__(NT, MINB) zy_pass(ZyArgs a) {
     C* q = br + x1 * NL + x;
     const int sw = x1 % S::zg;
 #pragma unroll
-    for (int k1 = 0; k1 < 8; ++k1) {
+    for (int k1 = 0; k1 < R; ++k1) {
       Dft<8, -1, float>::run(v[k1]);
 #pragma unroll
       for (int k2 = 1; k2 < 8; ++k2) v[k1][k2] = mul<float>(v[k1][k2], t[k2]);
@@ -464,18 +486,18 @@ __global__ void __launch_bounds__(NT, MINB) zy_pass(ZyArgs a) {
   }
   __syncthreads();
   // item (x, n1): z inverse stage A' (inverse DFT_8 over k2 per row: natural
-  // z = n1 + M n2), then y inverse stage B' (inverse DFT_8 over the rows,
+  // z = n1 + M n2), then y inverse stage B' (inverse DFT_R over the rows,
   // conjugate twiddle w_L^(ny k2y)) -> rows y0 + ny
-  C t[8];  // the brick's y twiddles (ny k2y < L)
+  C t[R];  // the brick's y twiddles (ny k2y < L)
 #pragma unroll
-  for (int ny = 1; ny < 8; ++ny) t[ny] = ty[ny * k2y];
+  for (int ny = 1; ny < R; ++ny) t[ny] = ty[ny * k2y];
   for (int i = tid; i < TX * M; i += NT) {
     const int x = i % TX, n1 = i / TX;
     const C* q = br + n1 * NL + x;
     const int sw = n1 % S::zg;
-    C u[8][8];
+    C u[R][8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
+    for (int r = 0; r < R; ++r) {
       const C* qr = q + (r ^ sw) * TX;
 #pragma unroll
       for (int k2 = 0; k2 < 8; ++k2) u[r][k2] = qr[k2 * (M * NL)];
@@ -484,14 +506,14 @@ __global__ void __launch_bounds__(NT, MINB) zy_pass(ZyArgs a) {
     C* p = g + (long long)n1 * zs + x;
 #pragma unroll
     for (int n2 = 0; n2 < 8; ++n2) {
-      C c[8];
+      C c[R];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) c[r] = u[r][n2];
-      Dft<8, +1, float>::run(c);
+      for (int r = 0; r < R; ++r) c[r] = u[r][n2];
+      Dft<R, +1, float>::run(c);
 #pragma unroll
-      for (int ny = 1; ny < 8; ++ny) c[ny] = mulc<float>(c[ny], t[ny]);
+      for (int ny = 1; ny < R; ++ny) c[ny] = mulc<float>(c[ny], t[ny]);
 #pragma unroll
-      for (int ny = 0; ny < 8; ++ny) p[(long long)(M * n2) * zs + (long long)ny * L] = c[ny];
+      for (int ny = 0; ny < R; ++ny) p[(long long)(M * n2) * zs + (long long)ny * L] = c[ny];
     }
   }
 }

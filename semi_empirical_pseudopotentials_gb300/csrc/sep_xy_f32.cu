@@ -72,9 +72,6 @@ int xy_split_n1(int L) {
   return 0;
 }
 
-// y is split 8 x (L / 8) by both forms (the plane lengths have N1 = 8)
-int xy_split_y(int L) { return xy_split_n1(L) > 0 ? 8 : 0; }
-
 namespace {
 bool plane_length(int L) {
 #define SEP_XY_IS(LL) \
@@ -83,19 +80,31 @@ bool plane_length(int L) {
 #undef SEP_XY_IS
   return false;
 }
+
+// 2: sub-plane form, 1: plane form, 0: none
+int xy_form(int nx, int ny, int nz) {
+  if (nx != ny) return 0;
+  if (nz == nx && subplane_length(nx)) return 2;
+  return plane_length(nx) ? 1 : 0;
+}
 }  // namespace
 
+// y: R x (L / R) in the sub-plane form, the plane pass's N1 = 8 otherwise
+int xy_split_y(int nx, int nz) {
+  const int f = xy_form(nx, nx, nz);
+  return f == 2 ? subplane_rows(nx) : (f == 1 ? xy_split_n1(nx) : 0);
+}
+
 bool xy_supported(const GridDev<float>& g) {
-  if (g.nx != g.ny || !g.kxr || !g.kyr) return false;
-  return plane_length(g.nx) || (subplane_length(g.nx) && g.nz == g.nx);
+  return g.kxr && g.kyr && xy_form(g.nx, g.ny, g.nz) > 0;
 }
 
 cudaError_t xy_prepare(const GridDev<float>& g) {
+  if (xy_form(g.nx, g.ny, g.nz) == 2) return subplane_prepare(g.nx);
 #define SEP_XY_PREP(LL) \
   if (g.nx == LL) return prepare_len<LL>();
   SEP_XY_LENGTHS(SEP_XY_PREP)
 #undef SEP_XY_PREP
-  if (subplane_length(g.nx)) return subplane_prepare(g.nx);
   return cudaErrorInvalidValue;
 }
 
@@ -115,11 +124,13 @@ cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& 
   a.nx = g.nx;
   a.ny = g.ny;
   a.nz = g.nz;
+  const int form = xy_form(g.nx, g.ny, g.nz);
+  if (form == 2) return subplane_launch(mode, a, B, s);
+  if (form != 1) return cudaErrorInvalidValue;
 #define SEP_XY_RUN(LL) \
   if (g.nx == LL) return launch_mode<LL>(mode, a, B, s);
   SEP_XY_LENGTHS(SEP_XY_RUN)
 #undef SEP_XY_RUN
-  if (subplane_length(g.nx)) return subplane_launch(mode, a, B, s);
   return cudaErrorInvalidValue;
 }
 
@@ -127,14 +138,13 @@ cudaError_t run_xy_pass(int mode, const GridDev<float>& g, const PassIO<float>& 
 // position order, or (sub-plane form) the zy pass
 cudaError_t run_xy_zpass(const GridDev<float>& g, const PassIO<float>& io, int B,
                          cudaStream_t s) {
-  if (plane_length(g.nx)) {
-    GridDev<float> gz = g;
-    gz.kx = g.kxr;
-    gz.ky = g.kyr;
-    return run_pass<float>(2, kFwdKInv, gz, io, B, s);
-  }
-  if (subplane_length(g.nx)) return zy_launch(g, io.data, B, s);
-  return cudaErrorInvalidValue;
+  const int form = xy_form(g.nx, g.ny, g.nz);
+  if (form == 2) return zy_launch(g, io.data, B, s);
+  if (form != 1) return cudaErrorInvalidValue;
+  GridDev<float> gz = g;
+  gz.kx = g.kxr;
+  gz.ky = g.kyr;
+  return run_pass<float>(2, kFwdKInv, gz, io, B, s);
 }
 
 }  // namespace sep
