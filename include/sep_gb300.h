@@ -74,15 +74,15 @@ int sep_ctx_stream(sep_ctx *ctx, void **cuda_stream);             /* cudaStream_
 int sep_ctx_set_graphs(sep_ctx *ctx, int enable);
 /* Newton steps accumulated per pass over the step history (default 32). */
 int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
-/* Complex64 Newton steps take two grid passes instead of four.  On grids
- * with nx = ny in {40, 48, 56, 64, 72, 80, 96, 112, 128}: the z line pass and
- * one fused pass per z-plane for the x and y transforms and the epilogue (same
- * arithmetic per line as the line passes).  On grids with nx = ny = nz in
- * {160, 192, 256}: a z pass that also does the y transform's 8-point stage,
- * and a fused pass per sub-plane of L / 8 rows for the rest of the y
- * transform, the x transforms and the epilogue (same transforms with y and z
- * split differently: equal to the line passes within FP32 rounding).
- * enable = 0 selects the four line passes.  Default 1. */
+/* Complex64 Newton steps take two grid passes instead of four.  On cubic
+ * grids with nx in {96, 112, 128, 160, 192, 256}: a z pass that also does the
+ * y transform's R-point stage (R = 4 or 8), and a fused pass per sub-plane of
+ * L / R rows for the rest of the y transform, the x transforms and the
+ * epilogue (same transforms with y and z split differently: equal to the line
+ * passes within FP32 rounding).  On other grids with nx = ny in {40, 48, 56,
+ * 64, 72, 80, 96, 112, 128}: the z line pass and one fused pass per z-plane
+ * for the x and y transforms and the epilogue (same arithmetic per line as
+ * the line passes).  enable = 0 selects the four line passes.  Default 1. */
 int sep_ctx_set_fusion(sep_ctx *ctx, int enable);
 /* FP64 refinement steps (0..8, default 0) that sep_pipeline runs after
  * Rayleigh-Ritz (filter/Hmat.c:11-86).  Each step extends the subspace with

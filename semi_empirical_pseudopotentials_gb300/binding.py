@@ -428,9 +428,10 @@ class Context:
         _check(lib().sep_ctx_set_eigensolver(self.h, int(m)))
 
     def set_fusion(self, enable):
-        """Fused two-pass complex64 Newton steps: the xy plane pass for nx = ny in
-        {40, 48, ..., 128}, the sub-plane and zy passes for nx = ny = nz in
-        {160, 192, 256}.  On by default; off: the four line passes."""
+        """Fused two-pass complex64 Newton steps: the sub-plane and zy passes for
+        cubic grids with nx in {96, 112, 128, 160, 192, 256}, else the xy plane
+        pass for nx = ny in {40, 48, ..., 128}.  On by default; off: the four
+        line passes."""
         _check(lib().sep_ctx_set_fusion(self.h, 1 if enable else 0))
 
     def set_subspace(self, mode):

@@ -64,7 +64,7 @@ cudaError_t run_pass(int axis, int mode, const GridDev<T>& g, const PassIO<T>& i
 
 // Fused two-pass Newton step of complex64 grids with nx = ny: the xy pass
 // (modes kFwd, kInvEpi, kInvEpiFwd) and the z pass of that step.  Cubic grids
-// with nx in {128, 160, 192, 256} take the sub-plane form: the xy pass works
+// with nx in {96, 112, 128, 160, 192, 256} take the sub-plane form: the xy pass works
 // on sub-planes and the z pass also does the y transform's R-point stage
 // (sep_subplane.cuh).  Other grids with nx in {40, ..., 128} take the plane
 // form: the xy pass works on whole z-planes (sep_xypass.cuh) and the z pass is

@@ -1,5 +1,5 @@
 // sep_sp_f32.cu -- launch of the sub-plane pass and the zy pass (complex64),
-// the fused Newton step for nx = ny = nz in {128, 160, 192, 256}.
+// the fused Newton step for nx = ny = nz in {96, 112, 128, 160, 192, 256}.
 #include "sep_engine.cuh"
 #include "sep_subplane.cuh"
 
@@ -67,7 +67,7 @@ cudaError_t launch_sp_mode(int mode, const PassArgs<float>& a, int B, cudaStream
 
 }  // namespace
 
-#define SEP_SP_LENGTHS(X) X(128) X(160) X(192) X(256)
+#define SEP_SP_LENGTHS(X) X(96) X(112) X(128) X(160) X(192) X(256)
 
 bool subplane_length(int L) {
 #define SEP_SP_IS(LL) \

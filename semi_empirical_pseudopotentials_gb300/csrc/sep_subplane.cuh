@@ -1,13 +1,13 @@
 // sep_subplane.cuh -- the two-pass complex64 Newton step on sub-planes, for
-// cubic grids L^3 with L in {128, 160, 192, 256}: xy planes that do not fit
-// in one block's shared memory (a 192^2 plane is 295 KB), and 128^2 planes,
-// which fit only one per SM.
+// cubic grids L^3 with L in {96, 112, 128, 160, 192, 256}: xy planes that do
+// not fit in one block's shared memory (a 192^2 plane is 295 KB), and planes
+// of 96^2 to 128^2, of which one or two fit per SM.
 //
 // Each 1-D transform is a four-step split (sep_fftpass.cuh): for a length
 // L = N1 N2, forward stage A (per residue x1: DFT_N2 over x1 + N1 x2,
 // twiddle w_L^(x1 k2)) and stage B (per k2: DFT_N1 over x1 + N1 k2, element
 // k2 + N2 k1 left at position k1 + N1 k2); inverse stage B' then A'.  Here y
-// is split R x (L / R) (R = 4 for 128, 8 for 160, 192, 256) and z
+// is split R x (L / R) (R = 4 for 96 and 128, 8 for the others) and z
 // (LZ / 8) x 8.  Stage A of y only couples the L / R rows of one residue, and
 // stage B only R adjacent rows, so:
 //
@@ -36,9 +36,17 @@ namespace sep {
 // sub-plane pass launch shape per length: threads per block, blocks per SM,
 // whether the last stage of a unit runs with the first of the next (fastest
 // measured, step pass on 0.5 GB of grids, fraction of the copy bandwidth:
-// 128^2 0.84, 160^2 0.75, 192^2 0.84, 256^2 0.75)
+// 96^2 0.83, 112^2 0.74, 128^2 0.84, 160^2 0.75, 192^2 0.84, 256^2 0.75)
 template <int L> struct SpTune {
   static constexpr int nt = 128, min_blocks = 4;
+  static constexpr bool fuse_next = true;
+};
+template <> struct SpTune<96> {
+  static constexpr int nt = 96, min_blocks = 5;
+  static constexpr bool fuse_next = true;
+};
+template <> struct SpTune<112> {
+  static constexpr int nt = 64, min_blocks = 6;
   static constexpr bool fuse_next = true;
 };
 template <> struct SpTune<128> {  // 32-row sub-planes: the fused column stage spills
@@ -62,6 +70,9 @@ template <> struct SpTune<256> {
 template <int L> struct SpRows {
   static constexpr int r = 8;
 };
+template <> struct SpRows<96> {
+  static constexpr int r = 4;
+};
 template <> struct SpRows<128> {
   static constexpr int r = 4;
 };
@@ -72,15 +83,16 @@ template <int L, int NT> struct SpShape {
   static constexpr int rows = n2y;  // rows of a sub-plane
   static constexpr int rs = L + 1;  // row stride (elements): rows 2 banks apart
   static constexpr int nt = NT;
-  static_assert(L % 16 == 0 && n2 == 16 && n2y <= 32, "sub-plane shapes");
+  static_assert(L % 16 == 0 && n2 <= 16 && n2y <= 32, "sub-plane shapes");
   static constexpr size_t smem_bytes = ((size_t)rows * rs + L) * sizeof(cx<float>);
 };
 
 // zy pass shape per length: TX adjacent columns per brick, threads per block,
 // blocks per SM.  A thread holds a 64-element block (about 160 registers); the
 // brick is LZ x 8 TX elements (33 to 131 KB).  Fastest measured (zy pass on
-// 0.5 GB of grids, fraction of the copy bandwidth): 128^3 (R = 4) TX 8 0.74,
-// 160^3 TX 4 0.48, 192^3 TX 4 0.51, 256^3 TX 8 0.40.  With R = 8 the pass is
+// 0.5 GB of grids, fraction of the copy bandwidth): 96^3 (R = 4) TX 8 0.75,
+// 112^3 TX 8 0.64, 128^3 (R = 4) TX 8 0.74, 160^3 TX 4 0.48, 192^3 TX 4
+// 0.51, 256^3 TX 8 0.40.  With R = 8 the pass is
 // issue-bound (about 60 FP32 instructions per element for the two 8-point y
 // stages and the z transform pair) with 12 warps per SM; R = 4 needs about
 // 90 registers and no multiplies in its y stages.

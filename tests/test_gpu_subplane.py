@@ -1,5 +1,5 @@
 """The fused complex64 Newton step in its sub-plane form (cubic grids with
-L in {128, 160, 192, 256}): the zy pass (the y transform's R-point stage, z
+L in {96, 112, 128, 160, 192, 256}): the zy pass (the y transform's R-point stage, z
 forward, k^2, z inverse) and the sub-plane pass (the rest of the y transform,
 x inverse, epilogue, x forward) against the four line passes that apply the
 same operator (filter/hamiltonian.c:27-44, filter/hnorm.c:11-39 inside
@@ -66,11 +66,11 @@ def test_subplane_pass_timing_slots():
     ctx.close()
 
 
-@pytest.mark.parametrize("dims", [(128, 128, 128)])
-def test_subplane_form_at_128_matches_the_line_passes(dims):
-    """Cubic 128^3 grids take the sub-plane form (y split 4 x 32); grids with
-    nz != 128 keep the plane form, which equals the line passes bit for bit
-    (tests/test_gpu_batch.py)."""
+@pytest.mark.parametrize("dims", [(96, 96, 96), (112, 112, 112), (128, 128, 128)])
+def test_subplane_form_at_96_to_128_matches_the_line_passes(dims):
+    """Cubic 96^3, 112^3 and 128^3 grids take the sub-plane form (y split 4 x 24,
+    8 x 14, 4 x 32); grids with nz != nx keep the plane form, which equals the
+    line passes bit for bit (tests/test_gpu_batch.py)."""
     ctx, pot, dv, n = _job(dims[0], 5)
     vmin = float(pot.min())
     emax, dE, _ = ctx.energy_range(vmin)
