@@ -274,13 +274,14 @@ def subspace_gram(sep, ctx, psi_d, m, n, dv, peaks):
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum per pair, 128^3 complex64,
 # from the captures summarised in profiles/line_pass_c64_128.md (12 pairs)
-# and profiles/xy_plane_pass_c64_128.md (6 pairs)
+# and profiles/subplane_zy_c64_128.md (6 pairs; the cubic 128^3 grid takes the
+# sub-plane form of the fused step)
 TRAFFIC_PER_PAIR_128 = {"y_fwd": (201.354752e6 + 142.915584e6) / 12,
                         "z_fki": (201.357312e6 + 140.684032e6) / 12,
                         "y_inv": (201.346304e6 + 143.166208e6) / 12,
                         "x_inv_epi_fwd": (444.561152e6 + 351.911936e6) / 12,
-                        # profiles/xy_plane_pass_c64_128.md (6 pairs)
-                        "xy_inv_epi_fwd": (209.92256e6 + 147.293952e6) / 6}
+                        "xy_inv_epi_fwd": (219.523072e6 + 148.553728e6) / 6,
+                        "xy_z": (100.69888e6 + 44.843776e6) / 6}
 
 
 def algorithmic_bytes(kind, npairs, n, c, r, ms=8, kblock=32):
