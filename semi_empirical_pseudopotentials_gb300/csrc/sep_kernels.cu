@@ -151,6 +151,94 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
   }
 }
 
+// Complex64 history, FP32 accumulators and exactly MS targets (the common
+// case): as k_accumulate, with two adjacent grid points per thread (16-byte
+// history loads) and the coefficients of four steps per 16-byte shared load,
+// so that the shared-memory pipe issues a quarter of the loads per multiply-
+// add.  Each point's sums take the same products in the same order as in
+// k_accumulate, so the results are equal bit for bit.  n is even.
+template <int MS>
+__global__ void __launch_bounds__(kThreads)
+k_accumulate_x2(const float4* __restrict__ hist, int slots, int B, long long n2, long long j0,
+                int count, const float* __restrict__ an, long long nc,
+                float* __restrict__ acc, int init) {
+  __shared__ __align__(16) float cf[MS * kMaxBlockSteps];
+  __shared__ long long soff[kMaxBlockSteps];  // in float4 (point pairs)
+  for (int i = threadIdx.x; i < MS * count; i += blockDim.x) {
+    const int e = i / count, s = i - e * count;
+    cf[e * kMaxBlockSteps + s] = an[e * nc + j0 + s];
+  }
+  const long long b = blockIdx.y;
+  for (int s = threadIdx.x; s < count; s += blockDim.x)
+    soff[s] = (long long)((j0 + s) % slots) * ((long long)B * n2) + b * n2;
+  __syncthreads();
+  for (long long g2 = blockIdx.x * (long long)blockDim.x + threadIdx.x; g2 < n2;
+       g2 += (long long)gridDim.x * blockDim.x) {
+    float re0[MS], im0[MS], re1[MS], im1[MS];
+#pragma unroll
+    for (int e = 0; e < MS; ++e) re0[e] = im0[e] = re1[e] = im1[e] = 0.f;
+    constexpr int LB = kLoadBatch;
+    int s = 0;
+    for (; s + LB <= count; s += LB) {
+      float4 h[LB];  // (x, y) of point 2 g2, then of point 2 g2 + 1
+#pragma unroll
+      for (int u = 0; u < LB; ++u) h[u] = hist[soff[s + u] + g2];
+#pragma unroll
+      for (int e = 0; e < MS; ++e) {
+        float c[LB];
+#pragma unroll
+        for (int q = 0; q < LB / 4; ++q) {
+          const float4 c4 = *reinterpret_cast<const float4*>(&cf[e * kMaxBlockSteps + s + 4 * q]);
+          c[4 * q] = c4.x;
+          c[4 * q + 1] = c4.y;
+          c[4 * q + 2] = c4.z;
+          c[4 * q + 3] = c4.w;
+        }
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+          re0[e] += c[u] * h[u].x;
+          im0[e] += c[u] * h[u].y;
+          re1[e] += c[u] * h[u].z;
+          im1[e] += c[u] * h[u].w;
+        }
+      }
+    }
+    for (; s < count; ++s) {
+      const float4 h = hist[soff[s] + g2];
+#pragma unroll
+      for (int e = 0; e < MS; ++e) {
+        const float c = cf[e * kMaxBlockSteps + s];
+        re0[e] += c * h.x;
+        im0[e] += c * h.y;
+        re1[e] += c * h.z;
+        im1[e] += c * h.w;
+      }
+    }
+    // the 2 MS accumulators of (pair b, point g): targets of state 2b, then
+    // of state 2b + 1; points 2 g2 and 2 g2 + 1 are adjacent
+    float4* p4 = reinterpret_cast<float4*>(acc + (b * 2 * n2 + 2 * g2) * (2 * MS));
+#pragma unroll
+    for (int pt = 0; pt < 2; ++pt) {
+#pragma unroll
+      for (int q = 0; q < MS / 2; ++q) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = 4 * q + u;
+          v[u] = pt == 0 ? (k < MS ? re0[k] : im0[k - MS]) : (k < MS ? re1[k] : im1[k - MS]);
+        }
+        float4 o = make_float4(v[0], v[1], v[2], v[3]);
+        float4* dst = p4 + pt * (MS / 2) + q;
+        if (!init) {
+          const float4 old = *dst;
+          o = make_float4(old.x + o.x, old.y + o.y, old.z + o.z, old.w + o.w);
+        }
+        *dst = o;
+      }
+    }
+  }
+}
+
 // accumulators [B][n][2 ms] -> out[(2b + c) ms + e][g] (state-major, double)
 template <typename TA>
 __global__ void k_unpack_acc(const TA* __restrict__ acc, long long B, long long n, int ms,
@@ -489,6 +577,13 @@ cudaError_t newton_accumulate(const cx<T>* hist, int slots, int B, long long n, 
   if (per > 65535) per = 65535;
   if (per < 1) per = 1;
   const dim3 g((unsigned)per, (unsigned)B);
+  if constexpr (std::is_same<T, float>::value && std::is_same<TA, float>::value) {
+    if (n % 2 == 0 && ms == 8) {  // two points per thread
+      k_accumulate_x2<8><<<g, kThreads, 0, s>>>(reinterpret_cast<const float4*>(hist), slots,
+                                                 B, n / 2, j0, count, an, nc, acc, init);
+      return cudaGetLastError();
+    }
+  }
   if (ms <= 4)
     k_accumulate<T, TA, 4><<<g, kThreads, 0, s>>>(hist, slots, B, n, j0, count, an, nc, ms, acc,
                                                   nstates, init);

@@ -105,3 +105,24 @@ def test_host_filter_in_chunks_equals_device_filter(precision, ns):
     ctx.filter_dev(sd.data_ptr(), ns, ar, zn, 4.0 / dE, vmin, od.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(host, od.cpu().numpy())
+
+
+@pytest.mark.parametrize("dims,K", [((40, 40, 40), 32), ((36, 40, 48), 64)])
+def test_two_point_accumulation_equals_the_generic_kernel(dims, K):
+    """The complex64 accumulation with 8 targets (k_accumulate_x2: two grid
+    points per thread, coefficients read four steps at a time) takes the same
+    products in the same order as the generic kernel, which a 9-target filter
+    uses: the 8-target filter equals the first 8 targets of the 9-target one
+    bit for bit.  nc = 70 leaves a last block of 6 steps (K = 32) or 5 (K =
+    64), so the kernels' tails run too."""
+    ctx, pot, dv, npts = _job(dims, 4, "mixed")
+    ctx.set_block_steps(K)
+    vmin = float(pot.min())
+    nc, dE = 70, 40.0
+    ar, ai, zn = sep.coefficients(np.linspace(-1.2, -0.2, 9), nc, dE, vmin,
+                                  (nc / (2.5 * dE)) ** 2)
+    start = sep.start_states(-13, 5, npts, dv)
+    out9 = ctx.filter(start, ar, zn, 4.0 / dE, vmin)
+    out8 = ctx.filter(start, np.ascontiguousarray(ar[:8]), zn, 4.0 / dE, vmin)
+    ctx.close()
+    assert np.array_equal(out8, out9[:, :8])
