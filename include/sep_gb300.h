@@ -110,6 +110,19 @@ int sep_ctx_set_refine(sep_ctx *ctx, int steps);
  * sep_timing.polish_s (also in total_s). */
 int sep_ctx_set_polish(sep_ctx *ctx, long nc, double guard);
 
+/* Arithmetic of the FP64-class work inside sep_pipeline: the H applies of
+ * Rayleigh-Ritz (filter/Hmat.c:11-86), of sigma (filter/energy.c:88-119) and
+ * of the residual refinement, and the Newton filter of the polish.
+ * mode 0: IEEE FP64 line passes (bound by the FP64 pipe on GB300).
+ * mode 1: double-float line passes, each value the unevaluated sum of two
+ * floats (about 48 significant bits; TwoSum / TwoProd with fused multiply-
+ * adds) on the FP32 pipe: an H apply about 3.7x faster at 128^3, within
+ * 2e-14 relative of the FP64 result.  States stay FP64 in memory between the
+ * stages.  Default 1 for complex64 contexts, 0 for FP64 contexts (whose
+ * pipeline is the FP64 reference).  sep_filter* in FP64 contexts, the
+ * energy range, sep_hamiltonian and sep_energy_all always use FP64. */
+int sep_ctx_set_arith(sep_ctx *ctx, int mode);
+
 /* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------
  * hpsi = T psi + V psi for nstates complex grids (interleaved complex128). */
 int sep_hamiltonian(sep_ctx *ctx, const double *psi, double *hpsi, long nstates);

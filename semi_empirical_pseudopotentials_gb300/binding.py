@@ -82,6 +82,7 @@ def lib():
                                           C.c_long, dp, dp, dp, dp]
         L.sep_time_passes.argtypes = [vp, C.c_long, C.c_int, dp]
         L.sep_time_fused_step.argtypes = [vp, C.c_long, C.c_int, dp]
+        L.sep_ctx_set_arith.argtypes = [vp, C.c_int]
         L.sep_hf_density.argtypes = [vp, dp, C.c_long, dp, dp]
         L.sep_ctx_autotune.argtypes = [vp, C.c_long, C.c_int, ip]
         L.sep_batch_create.argtypes = [C.c_int, C.POINTER(vp), lp, C.c_long, C.c_long,
@@ -433,6 +434,13 @@ class Context:
         pass for nx = ny in {40, 48, ..., 128}.  On by default; off: the four
         line passes."""
         _check(lib().sep_ctx_set_fusion(self.h, 1 if enable else 0))
+
+    def set_arith(self, mode):
+        """Arithmetic of the pipeline's FP64-class H applies (Rayleigh-Ritz, sigma,
+        refinement, polish filter): "f64" (IEEE FP64) or "dd" (double-float on
+        the FP32 pipe, about 48 significant bits; default for complex64
+        contexts)."""
+        _check(lib().sep_ctx_set_arith(self.h, {"f64": 0, "dd": 1}[mode]))
 
     def set_subspace(self, mode):
         """Subspace contractions on the tensor cores ("tc", default) or the FP64 pipe ("f64")."""

@@ -24,6 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 CUDA_UNITS = ["sep_pass_f64.cu", "sep_pass_f32.cu", "sep_pass_f64_v1.cu", "sep_pass_f32_v1.cu",
+              "sep_pass_dd.cu", "sep_pass_dd_g0.cu", "sep_pass_dd_g1.cu", "sep_pass_dd_g2.cu",
+              "sep_pass_dd_g3.cu",
               "sep_xy_f32.cu", "sep_sp_f32.cu",
               "sep_kernels.cu", "sep_ctx.cu",
               "sep_api.cu", "sep_vbuild.cu", "sep_noalloc.cu",

@@ -85,6 +85,21 @@ template <typename T> int upload_grid(sep_ctx* c, GridDev<T>& g) {
   return kOk;
 }
 
+}  // namespace
+
+namespace sep {
+// the grid's tables and V in double-float, uploaded on first use
+int ensure_dd_grid(sep_ctx* c) {
+  if (c->dd_ready) return kOk;
+  RET(upload_grid<ddf>(c, c->gdd));
+  if (c->have_pot) CK(convert_f64_to_dd(c->g64.pot, c->gdd.pot, c->n, c->stream));
+  c->dd_ready = true;
+  return kOk;
+}
+}  // namespace sep
+
+namespace {
+
 int check_ctx(sep_ctx* c, bool need_pot = true) {
   if (!c) return arg_fail("null context");
   if (need_pot && !c->have_pot) return arg_fail("the context has no potential yet");
@@ -97,6 +112,7 @@ int install_potential(sep_ctx* c, const double* d_pot) {
   CK(cudaMemcpyAsync(c->g64.pot, d_pot, sizeof(double) * c->n, cudaMemcpyDeviceToDevice,
                      c->stream));
   if (c->precision == 1) CK(convert_f64_to_f32(c->g64.pot, c->g32.pot, c->n, c->stream));
+  if (c->dd_ready) CK(convert_f64_to_dd(c->g64.pot, c->gdd.pot, c->n, c->stream));
   std::vector<double> h(c->n);
   CK(cudaMemcpyAsync(h.data(), c->g64.pot, sizeof(double) * c->n, cudaMemcpyDeviceToHost,
                      c->stream));
@@ -143,6 +159,7 @@ sep_ctx::~sep_ctx() {
     if (g.exec) cudaGraphExecDestroy(g.exec);
   free_grid(g64);
   free_grid(g32);
+  free_grid(gdd);
   w_refine.release();
   for (DevBuf* b : {&w_hist, &w_fft, &w_acc, &w_coef, &w_steps, &w_start, &w_out, &w_red,
                     &w_small, &w_states, &w_states2, &w_tmp, &w_solver, &w_gemm, &w_hpsi,
@@ -194,6 +211,7 @@ int sep_ctx_create(const long dims[3], const double steps[3], double ekinmax,
   sep_ctx* c = new sep_ctx();
   cudaGetDevice(&c->device);
   c->precision = precision;
+  c->dd_arith = precision == 1 ? 1 : 0;
   c->nx = dims[0];
   c->ny = dims[1];
   c->nz = dims[2];
@@ -649,6 +667,12 @@ int sep_ctx_set_polish(sep_ctx* c, long nc, double guard) {
     return arg_fail("sep_ctx_set_polish: nc in {0} or [2, 8192] and a finite guard >= 0");
   c->polish_nc = nc;
   c->polish_guard = guard;
+  return kOk;
+}
+
+int sep_ctx_set_arith(sep_ctx* c, int mode) {
+  if (!c || (mode != 0 && mode != 1)) return arg_fail("sep_ctx_set_arith: mode is 0 or 1");
+  c->dd_arith = mode;
   return kOk;
 }
 

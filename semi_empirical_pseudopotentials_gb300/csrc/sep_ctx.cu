@@ -128,6 +128,13 @@ template <> struct Prec<double> {
 template <> struct Prec<float> {
   static GridDev<float>& grid(sep_ctx* c) { return c->g32; }
 };
+template <> struct Prec<ddf> {
+  static GridDev<ddf>& grid(sep_ctx* c) { return c->gdd; }
+};
+// tag of the precision in the filter graph cache (ddf and double are both 8 bytes)
+template <typename T> constexpr long long prec_tag() {
+  return std::is_same<T, ddf>::value ? 9 : (long long)sizeof(T);
+}
 
 // the fused xy plane pass runs complex64 Newton steps on square xy planes
 template <typename T> bool use_xy(sep_ctx*) { return false; }
@@ -326,7 +333,7 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
     if (c->use_graphs) {
       const long long key[8] = {bc, nst, ms, nc, K, (long long)(size_t)c->w_hist.p,
                                 (long long)(size_t)c->w_acc.p,
-                                (long long)sizeof(T) + (fused ? 256 : 0)};
+                                prec_tag<T>() + (fused ? 256 : 0)};
       FilterGraph* hit = nullptr;
       for (auto& fg : c->graphs)
         if (std::memcmp(fg.key, key, sizeof key) == 0) hit = &fg;
@@ -385,32 +392,46 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
   return rc;
 }
 
-// complex states through H in chunks that fit the scratch
-int apply_h_chunked(sep_ctx* c, const cx<double>* in, cx<double>* out, long long nst) {
+// complex states through H in chunks that fit the scratch (FP64 or its
+// double-float form: both 16 bytes per complex value)
+template <typename T>
+int apply_h_chunked_t(sep_ctx* c, const cx<T>* in, cx<T>* out, long long nst) {
   const long long n = c->n;
   long long chunk = (long long)((0.25 * (double)free_device_bytes() + c->w_fft.bytes) /
-                                (sizeof(cx<double>) * (double)n));
+                                (sizeof(cx<T>) * (double)n));
   if (chunk < 1) return arg_fail("hamiltonian: not enough device memory");
   chunk = std::min<long long>(chunk, std::min<long long>(nst, 4096));
-  RET(grow(c, c->w_fft, sizeof(cx<double>) * (size_t)n * chunk));
+  RET(grow(c, c->w_fft, sizeof(cx<T>) * (size_t)n * chunk));
   for (long long b0 = 0; b0 < nst; b0 += chunk) {
     const int bc = (int)std::min<long long>(chunk, nst - b0);
-    CK(apply_h<double>(c->g64, in + b0 * n, out + b0 * n, c->w_fft.as<cx<double>>(), bc, 1.0,
-                       0.0, c->stream));
+    CK(apply_h<T>(Prec<T>::grid(c), in + b0 * n, out + b0 * n, c->w_fft.as<cx<T>>(), bc, T(1.0),
+                  T(0.0), c->stream));
   }
   return kOk;
 }
+int apply_h_chunked(sep_ctx* c, const cx<double>* in, cx<double>* out, long long nst) {
+  return apply_h_chunked_t<double>(c, in, out, nst);
+}
 
-// H applied to m real states (rows of psi) -> hpsi rows, via pair packing
-int apply_h_real(sep_ctx* c, const double* d_psi, double* d_hpsi, long long m) {
+// H applied to m real states (rows of psi) -> hpsi rows, via pair packing;
+// in double-float when the context says so (FP64 in and out either way)
+template <typename T>
+int apply_h_real_t(sep_ctx* c, const double* d_psi, double* d_hpsi, long long m) {
   const long long n = c->n;
   const long long B = (m + 1) / 2;
-  RET(grow(c, c->w_states, sizeof(cx<double>) * (size_t)n * B));
-  RET(grow(c, c->w_states2, sizeof(cx<double>) * (size_t)n * B));
-  CK(pack_pairs<double, double>(d_psi, m, n, c->w_states.as<cx<double>>(), c->stream));
-  RET(apply_h_chunked(c, c->w_states.as<cx<double>>(), c->w_states2.as<cx<double>>(), B));
-  CK(unpack_pairs<double, double>(c->w_states2.as<cx<double>>(), m, n, d_hpsi, c->stream));
+  RET(grow(c, c->w_states, sizeof(cx<T>) * (size_t)n * B));
+  RET(grow(c, c->w_states2, sizeof(cx<T>) * (size_t)n * B));
+  CK(pack_pairs<T, double>(d_psi, m, n, c->w_states.as<cx<T>>(), c->stream));
+  RET(apply_h_chunked_t<T>(c, c->w_states.as<cx<T>>(), c->w_states2.as<cx<T>>(), B));
+  CK(unpack_pairs<T, double>(c->w_states2.as<cx<T>>(), m, n, d_hpsi, c->stream));
   return kOk;
+}
+int apply_h_real(sep_ctx* c, const double* d_psi, double* d_hpsi, long long m) {
+  if (c->dd_arith) {
+    RET(ensure_dd_grid(c));
+    return apply_h_real_t<ddf>(c, d_psi, d_hpsi, m);
+  }
+  return apply_h_real_t<double>(c, d_psi, d_hpsi, m);
 }
 
 // (T + shift)^-1 applied to m real states (rows of x), in place, via pair
@@ -933,8 +954,14 @@ int polish_device(sep_ctx* c, double* d_psi, long* k, double elmin, double elmax
   const double dt = ((double)nc / (2.5 * dE)) * ((double)nc / (2.5 * dE));  // main.c:70
   std::vector<double> ar((size_t)nc), ai((size_t)nc), zn((size_t)nc);
   host::coefficients(1, nc, dE, vmin, dt, &center, ar.data(), ai.data(), zn.data());
-  RET(filter_impl<double>(c, d_psi + (size_t)i0 * n, kb, ar.data(), zn.data(), 1, nc,
-                          4.0 / dE, vmin, F, nullptr));
+  if (c->dd_arith) {
+    RET(ensure_dd_grid(c));
+    RET(filter_impl<ddf>(c, d_psi + (size_t)i0 * n, kb, ar.data(), zn.data(), 1, nc, 4.0 / dE,
+                         vmin, F, nullptr));
+  } else {
+    RET(filter_impl<double>(c, d_psi + (size_t)i0 * n, kb, ar.data(), zn.data(), 1, nc,
+                            4.0 / dE, vmin, F, nullptr));
+  }
   RET(normalize_device(c, F, kb));
   long kb2 = 0;
   RET(ortho_device(c, F, kb, &kb2));

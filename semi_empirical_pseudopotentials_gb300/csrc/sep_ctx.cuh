@@ -87,6 +87,13 @@ struct sep_ctx {
   sep::host::KTables ktab;
   sep::GridDev<double> g64;
   sep::GridDev<float> g32;
+  // FP64-class arithmetic of the pipeline's Rayleigh-Ritz, sigma, refinement
+  // and polish H applies: IEEE FP64 (0) or double-float (1, sep_dd.cuh; the
+  // default for complex64 contexts); gdd holds the grid's tables and V in
+  // double-float once it is first needed
+  int dd_arith = 0;
+  bool dd_ready = false;
+  sep::GridDev<sep::ddf> gdd;
   // workspace
   sep::DevBuf w_refine;  // psi and its residual directions (refine_device)
   // spin-orbit operator of the spinor path (sep_spinor_set_operator): the
@@ -150,6 +157,7 @@ int sigma_device(sep_ctx* c, const double* d_psi, long m, double* sige_host,
 int normalize_device(sep_ctx* c, double* d_psi, long m, double* also = nullptr);
 int time_passes_device(sep_ctx* c, long npairs, int reps, double* ms_out);
 int time_fused_step_device(sep_ctx* c, long npairs, int reps, double* ms_out);
+int ensure_dd_grid(sep_ctx* c);  // uploads c->gdd (sep_api.cu)
 int subspace_gemm_device(sep_ctx* c, const double* A, const double* B, long long m, long long n,
                          long long k, double alpha, bool sym, double* C);
 int subspace_rotate_device(sep_ctx* c, const double* W, const double* X, long long m,

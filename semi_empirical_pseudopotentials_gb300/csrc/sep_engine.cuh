@@ -11,11 +11,13 @@
 
 #include <cuda_runtime.h>
 
+#include "sep_dd.cuh"
 #include "sep_fftpass.cuh"
 
 namespace sep {
 
-// device tables of one grid in one precision
+// device tables of one grid in one precision (double, float, or ddf: the
+// double-float form of the FP64 passes, sep_dd.cuh)
 template <typename T> struct GridDev {
   int nx = 0, ny = 0, nz = 0;
   long long n = 0;

@@ -105,7 +105,9 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
     // the 2 ms accumulators of (pair b, point g) are adjacent: targets of
     // state 2b, then of state 2b + 1
     TA* __restrict__ pa = acc + (b * n + g) * (2 * ms);
-    if (std::is_same<TA, float>::value && MSMAX <= 16 && ms == MSMAX) {
+    bool stored = false;
+    if constexpr (std::is_same<TA, float>::value) {
+    if (MSMAX <= 16 && ms == MSMAX) {
       float4* p4 = reinterpret_cast<float4*>(pa);
 #pragma unroll
       for (int q = 0; q < MSMAX / 2; ++q) {
@@ -122,7 +124,7 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
         }
         p4[q] = o;
       }
-    } else if (std::is_same<TA, float>::value && ms % 2 == 0) {
+    } else if (ms % 2 == 0) {
       float2* q0 = reinterpret_cast<float2*>(pa);
       float2* q1 = reinterpret_cast<float2*>(pa + ms);
 #pragma unroll
@@ -139,7 +141,10 @@ k_accumulate(const cx<T>* __restrict__ hist, int slots, int B, long long n, long
           q1[e / 2] = i;
         }
       }
-    } else {
+    }
+    stored = (MSMAX <= 16 && ms == MSMAX) || ms % 2 == 0;
+    }
+    if (!stored) {
 #pragma unroll
       for (int e = 0; e < MSMAX; ++e) {
         if (e < ms) {
@@ -564,6 +569,10 @@ template cudaError_t unpack_pairs<float, double>(const cx<float>*, long long, lo
                                                  cudaStream_t);
 template cudaError_t unpack_pairs<float, float>(const cx<float>*, long long, long long, float*,
                                                 cudaStream_t);
+template cudaError_t pack_pairs<ddf, double>(const double*, long long, long long, cx<ddf>*,
+                                             cudaStream_t);
+template cudaError_t unpack_pairs<ddf, double>(const cx<ddf>*, long long, long long, double*,
+                                               cudaStream_t);
 
 template <typename T, typename TA>
 cudaError_t newton_accumulate(const cx<T>* hist, int slots, int B, long long n, long long j0,
@@ -606,6 +615,9 @@ template cudaError_t newton_accumulate<float, float>(const cx<float>*, int, int,
                                                      long long, int, const float*, long long,
                                                      int, float*, long long, bool,
                                                      cudaStream_t);
+template cudaError_t newton_accumulate<ddf, ddf>(const cx<ddf>*, int, int, long long, long long,
+                                                 int, const ddf*, long long, int, ddf*,
+                                                 long long, bool, cudaStream_t);
 
 template <typename TA>
 cudaError_t unpack_accumulators(const TA* acc, long long B, long long n, int ms,
@@ -618,6 +630,8 @@ template cudaError_t unpack_accumulators<float>(const float*, long long, long lo
                                                 long long, double*, cudaStream_t);
 template cudaError_t unpack_accumulators<double>(const double*, long long, long long, int,
                                                  long long, double*, cudaStream_t);
+template cudaError_t unpack_accumulators<ddf>(const ddf*, long long, long long, int, long long,
+                                              double*, cudaStream_t);
 
 size_t reduce_partial_doubles(long long rows) { return (size_t)rows * kPartials * 2; }
 
@@ -844,6 +858,10 @@ cudaError_t convert_f32_to_f64(const float* in, double* out, long long count, cu
 }
 cudaError_t convert_f64_to_f32(const double* in, float* out, long long count, cudaStream_t s) {
   k_convert<double, float><<<blocks_for(count, kThreads), kThreads, 0, s>>>(in, out, count);
+  return cudaGetLastError();
+}
+cudaError_t convert_f64_to_dd(const double* in, ddf* out, long long count, cudaStream_t s) {
+  k_convert<double, ddf><<<blocks_for(count, kThreads), kThreads, 0, s>>>(in, out, count);
   return cudaGetLastError();
 }
 

@@ -5,7 +5,7 @@
 
 #include <cuda_runtime.h>
 
-#include "sep_dft.cuh"
+#include "sep_dd.cuh"
 
 namespace sep {
 
@@ -95,5 +95,6 @@ cudaError_t residual_rows(const double* x, const double* hx, const double* e, lo
 // precision conversion
 cudaError_t convert_f32_to_f64(const float* in, double* out, long long count, cudaStream_t s);
 cudaError_t convert_f64_to_f32(const double* in, float* out, long long count, cudaStream_t s);
+cudaError_t convert_f64_to_dd(const double* in, ddf* out, long long count, cudaStream_t s);
 
 }  // namespace sep

@@ -2,6 +2,8 @@
 // precision (included by sep_pass_f64.cu and sep_pass_f32.cu with SEP_T set).
 #pragma once
 
+#include <type_traits>
+
 #include "sep_engine.cuh"
 
 namespace sep {
@@ -35,7 +37,7 @@ cudaError_t launch_len(int axis, int mode, const PassArgs<T>& a, int B, cudaStre
     if (mode == kInv) return launch_one<T, L, 1, kInv, V>(a, B, s);
   } else if (axis == 2) {
     if (mode == kFwdKInv) return launch_one<T, L, 2, kFwdKInv, V>(a, B, s);
-    if constexpr (sizeof(T) == 8)  // the preconditioner of the FP64 refinement
+    if constexpr (std::is_same<T, double>::value)  // the preconditioner of the FP64 refinement
       if (mode == kFwdPInv) return launch_one<T, L, 2, kFwdPInv, V>(a, B, s);
   }
   return cudaErrorInvalidValue;
@@ -57,6 +59,32 @@ cudaError_t launch_variant<SEP_T, SEP_V>(int axis, int mode, int L, const PassAr
     SEP_CASE(14) SEP_CASE(16) SEP_CASE(18) SEP_CASE(20) SEP_CASE(24) SEP_CASE(32) SEP_CASE(36)
     SEP_CASE(40) SEP_CASE(48) SEP_CASE(56) SEP_CASE(64) SEP_CASE(72) SEP_CASE(80)
     SEP_CASE(96) SEP_CASE(112) SEP_CASE(128) SEP_CASE(160) SEP_CASE(192) SEP_CASE(256)
+#undef SEP_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+#endif
+
+// The double-float passes (SEP_T = ddf, tile shape 0) compile in four
+// translation units of a few lengths each: their kernels unroll the
+// error-free operations into long straight-line code, and one unit with
+// every length took minutes.
+#define SEP_DD_GROUP0(X) X(14) X(16) X(18) X(20) X(24) X(32) X(36)
+#define SEP_DD_GROUP1(X) X(40) X(48) X(56) X(64) X(72) X(80)
+#define SEP_DD_GROUP2(X) X(96) X(112) X(128)
+#define SEP_DD_GROUP3(X) X(160) X(192) X(256)
+template <int G>
+cudaError_t launch_dd_group(int axis, int mode, int L, const PassArgs<ddf>& a, int B,
+                            cudaStream_t s);
+
+#ifdef SEP_DD_G
+template <>
+cudaError_t launch_dd_group<SEP_DD_G>(int axis, int mode, int L, const PassArgs<ddf>& a, int B,
+                                      cudaStream_t s) {
+  switch (L) {
+#define SEP_CASE(LL) \
+  case LL: return launch_len<ddf, LL, 0>(axis, mode, a, B, s);
+    SEP_DD_LIST(SEP_CASE)
 #undef SEP_CASE
     default: return cudaErrorInvalidValue;
   }
@@ -90,9 +118,19 @@ cudaError_t run_pass<SEP_T>(int axis, int mode, const GridDev<SEP_T>& g,
   a.ny = g.ny;
   a.nz = g.nz;
   const int L = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+#ifdef SEP_IS_DD  // double-float: tile shape 0 only, the lengths in four units
+#define SEP_DD_IN(LL) || L == LL
+  if (false SEP_DD_GROUP0(SEP_DD_IN)) return launch_dd_group<0>(axis, mode, L, a, B, s);
+  if (false SEP_DD_GROUP1(SEP_DD_IN)) return launch_dd_group<1>(axis, mode, L, a, B, s);
+  if (false SEP_DD_GROUP2(SEP_DD_IN)) return launch_dd_group<2>(axis, mode, L, a, B, s);
+  if (false SEP_DD_GROUP3(SEP_DD_IN)) return launch_dd_group<3>(axis, mode, L, a, B, s);
+#undef SEP_DD_IN
+  return cudaErrorInvalidValue;
+#else
   const int v = io.variant >= 0 ? io.variant : g.variant[pass_kind(axis, mode)];
   if (v == 1) return launch_variant<SEP_T, 1>(axis, mode, L, a, B, s);
   return launch_variant<SEP_T, 0>(axis, mode, L, a, B, s);
+#endif
 }
 
 template <>
