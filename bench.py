@@ -963,7 +963,7 @@ def large_case():
                                    f"({S.ngrid} points), {S.ns} start states x {S.ms} targets, "
                                    f"nc {S.nc}",
                        "precision": "complex64 filter, FP32 accumulation; FP64 ortho and "
-                                    "Rayleigh-Ritz"},
+                                    "Rayleigh-Ritz with double-float H applies"},
             "stages_s": {k: round(v, 3) for k, v in t.items() if k.endswith("_s")},
             "wall_s": wall,
             "filter_applies_per_s": S.ns * (S.nc - 1) / t["filter_s"],
