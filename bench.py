@@ -734,6 +734,27 @@ def run_sep(args):
         f1.synchronize()
         t64 = f0.elapsed_time(f1) * 1e-3
         per64 = ctx64.time_passes(npairs, reps=3)
+        # the same sample in double-float arithmetic (sep_ctx_set_arith), against
+        # the FP64 output just computed
+        ref64 = out_d.clone()
+        ctx64.set_arith("dd")
+        ctx64.filter_dev(start_d.data_ptr(), ns, an_re[:, :ncs], zn[:ncs], 4.0 / dE, vmin,
+                         out_d.data_ptr())
+        f0.record(s64)
+        ctx64.filter_dev(start_d.data_ptr(), ns, an_re[:, :ncs], zn[:ncs], 4.0 / dE, vmin,
+                         out_d.data_ptr())
+        f1.record(s64)
+        f1.synchronize()
+        tdd = f0.elapsed_time(f1) * 1e-3
+        extras["fp64_class_double_float"] = {
+            "value": ns * (ncs - 1) / tdd, "unit": "applies/s",
+            "sample": f"{ns} states x {ncs - 1} Newton steps (the FP64 sample's)",
+            "max_rel_diff_vs_fp64": float((out_d - ref64).abs().max() / ref64.abs().max()),
+            "speedup_over_fp64": t64 / tdd,
+            "note": "sep_ctx_set_arith(1) in an FP64 context: line passes in double-float "
+                    "(two floats per value, about 48 significant bits) on the FP32 pipe"}
+        del ref64
+        ctx64.set_arith("f64")
         extras["fp64"] = {"value": ns * (ncs - 1) / t64, "unit": "applies/s",
                           "sample": f"{ns} states x {ncs - 1} Newton steps",
                           "per_launch_ms": dict(zip(names[:7], [round(p, 4) for p in per64])),

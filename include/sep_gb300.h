@@ -119,8 +119,10 @@ int sep_ctx_set_polish(sep_ctx *ctx, long nc, double guard);
  * adds) on the FP32 pipe: an H apply about 3.7x faster at 128^3, within
  * 2e-14 relative of the FP64 result.  States stay FP64 in memory between the
  * stages.  Default 1 for complex64 contexts, 0 for FP64 contexts (whose
- * pipeline is the FP64 reference).  sep_filter* in FP64 contexts, the
- * energy range, sep_hamiltonian and sep_energy_all always use FP64. */
+ * pipeline is the FP64 reference).  In an FP64 context mode 1 also runs the
+ * Newton filter of sep_filter* and sep_pipeline in double-float (an FP64-
+ * class filter about 3.7x faster at 128^3).  The energy range,
+ * sep_hamiltonian and sep_energy_all always use FP64. */
 int sep_ctx_set_arith(sep_ctx *ctx, int mode);
 
 /* ---- Hamiltonian: filter/hamiltonian.c:11-44 -----------------------------

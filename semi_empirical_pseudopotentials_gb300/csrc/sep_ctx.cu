@@ -614,6 +614,10 @@ int filter_device(sep_ctx* c, const double* d_start, long ns, const double* an_r
   if (ns < 1 || ms < 1 || nc < 1 || ms > 32) return arg_fail("filter: need ns, nc >= 1 and 1 <= ms <= 32");
   if (c->precision == 1)
     return filter_impl<float>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out, host);
+  if (c->dd_arith) {  // an FP64 context that asked for double-float arithmetic
+    RET(ensure_dd_grid(c));
+    return filter_impl<ddf>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out, host);
+  }
   return filter_impl<double>(c, d_start, ns, an_re, zn, ms, nc, dE_1, vmin, d_out, host);
 }
 
