@@ -78,10 +78,12 @@ def parse():
     p.add_argument("--large", action="store_true",
                    help="one whole mixed pipeline on the 4 nm sphere: 192^3 grid, 256 start "
                         "states x 8 targets (about 250 GB on the device)")
-    p.add_argument("--profile", choices=["mixed", "f64", "subspace", "pipeline"], default=None,
+    p.add_argument("--profile", choices=["mixed", "f64", "dd", "subspace", "pipeline"],
+                   default=None,
                    help="run only a small case for an ncu capture: 24 (mixed) or 16 "
-                        "(f64) start states x 8 Newton steps of the 128^3 workload (3.5 GB "
-                        "and 4.8 GB on the device), or (subspace) the tensor-core Gram of "
+                        "(f64; dd: an FP64 context in double-float arithmetic) start states "
+                        "x 8 Newton steps of the 128^3 workload (3.5 GB and 4.8 GB on the "
+                        "device), or (subspace) the tensor-core Gram of "
                         "512 states x 262144 points (1.1 GB)), or (pipeline) one whole mixed "
                         "pipeline of the 128^3 workload for a launch list")
     return p.parse_args()
@@ -110,7 +112,9 @@ def run_profile(args):
                           "stages_s": {k: round(v, 3) for k, v in res["timing"].items()
                                        if k.endswith("_s")}}))
         return
-    ctx = sep.Context(S.dims, S.steps, precision=args.profile)
+    ctx = sep.Context(S.dims, S.steps, precision="f64" if args.profile == "dd" else args.profile)
+    if args.profile == "dd":
+        ctx.set_arith("dd")
     ctx.set_block_steps(8)
     ctx.set_graphs(False)
     ctx.vbuild(S.xyz, S.types.astype(np.int32), tr, tv, [1024, 1024], S.mins)

@@ -335,10 +335,12 @@ line_pass(PassArgs<T> a) {
       if ((NA % NT == 0 || i < NA) && line < nvalid) {
         const long long lb = base0 + line * lstride;          // offset in the batch array
         const long long gb = lb % N;                          // offset in one grid
-        const C* pin = a.psi_in ? a.psi_in + lb : nullptr;
-        const C* pex = a.extra ? a.extra + lb : nullptr;
-        C* pout = a.psi_out + lb;
-        const T* pv = a.pot + gb;
+        // psi_{j-1}, the extra term and V never alias psi_j: the loads of all
+        // n2 can go out ahead of the stores
+        const C* __restrict__ pin = a.psi_in ? a.psi_in + lb : nullptr;
+        const C* __restrict__ pex = a.extra ? a.extra + lb : nullptr;
+        C* __restrict__ pout = a.psi_out + lb;
+        const T* __restrict__ pv = a.pot + gb;
 #pragma unroll
         for (int n2 = 0; n2 < N2; ++n2) {
           const int x = n1 + N1 * n2;
