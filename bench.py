@@ -40,7 +40,7 @@ WORKLOAD = dict(name="r2.5nm_128", radius_nm=2.5, n=128, ms=8, ns=64, nc=1024, s
 # Newton steps per accumulation pass of the complex64 filter: 64 reads the
 # 8 accumulators of each point half as often as the library's default 32
 # (0.126 against 0.144 ms per step at 32 pairs) for 17 GB more history
-BLOCK_STEPS = 64
+BLOCK_STEPS = 128
 START_SEED = -271828
 # Time to band-edge eigenpairs, on a case where both precisions converge: the
 # same 2.5 nm sphere and 128^3 grid with the fitted CdSe form factors of the
@@ -60,7 +60,7 @@ def bench_config(world):
     """The `config` of both arms' JSON lines (the same workload)."""
     return {"workload": "r2.5nm CdSe-like sphere (2317 atoms), 128^3, 64 start states x "
                         "8 targets, nc 1024",
-            "l2": "inputs larger than L2 (about 45 GB of filter state)",
+            "l2": "inputs larger than L2 (about 87 GB of filter state)",
             "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
 
 

@@ -72,7 +72,8 @@ int sep_ctx_info(sep_ctx *ctx, double *vmin, double *vmax, double *dv, long *ngr
 int sep_ctx_stream(sep_ctx *ctx, void **cuda_stream);             /* cudaStream_t */
 /* Capture the Newton loop of sep_filter* in a CUDA graph (default 1). */
 int sep_ctx_set_graphs(sep_ctx *ctx, int enable);
-/* Newton steps accumulated per pass over the step history (default 32). */
+/* Newton steps accumulated per pass over the step history, 1 <= k <= 128
+ * (default 32; the history holds k grids per pair of states). */
 int sep_ctx_set_block_steps(sep_ctx *ctx, int k);
 /* Complex64 Newton steps take two grid passes instead of four.  On cubic
  * grids with nx in {96, 112, 128, 160, 192, 256}: a z pass that also does the

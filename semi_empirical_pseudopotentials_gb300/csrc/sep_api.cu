@@ -286,7 +286,7 @@ int sep_ctx_set_graphs(sep_ctx* c, int enable) {
 }
 
 int sep_ctx_set_block_steps(sep_ctx* c, int k) {
-  if (!c || k < 1 || k > 64) return arg_fail("sep_ctx_set_block_steps: 1 <= k <= 64");
+  if (!c || k < 1 || k > 128) return arg_fail("sep_ctx_set_block_steps: 1 <= k <= 128");
   c->block_steps = k;
   return kOk;
 }

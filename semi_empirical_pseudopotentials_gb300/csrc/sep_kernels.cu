@@ -45,7 +45,7 @@ __global__ void k_unpack(const cx<T>* __restrict__ in, long long nstates, long l
 }
 
 // -------------------------------------------------------------------------
-constexpr int kMaxBlockSteps = 64;  // history grids per accumulation pass
+constexpr int kMaxBlockSteps = 128;  // history grids per accumulation pass
 constexpr int kLoadBatch = 8;       // history loads in flight per thread (ms > 4)
 
 template <typename T, typename TA, int MSMAX>
