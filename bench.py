@@ -822,9 +822,9 @@ def run_sep(args):
 
     heavy = not args.no_extras and rank == 0 and world == 1
     if heavy:
-        # BASELINE configurations 2 and 4 on the same box, after the headline
-        # context has released its workspaces: 32 uneven nanocrystals in one
-        # launch against one after another, and the 4 nm sphere at 192^3
+        # the batched and the large-grid workloads on the same box, after the
+        # headline context has released its workspaces: 32 uneven nanocrystals
+        # in one launch against one after another, and the 4 nm sphere at 192^3
         del start_d
         ctx.close()
         ctx = None

@@ -1,8 +1,9 @@
-"""The large-grid configuration's path (the 4 nm sphere on a 192^3 grid, BASELINE
-configuration 4) on a small case: the Newton filter's line passes of length 192
-in both precisions against the oracle (filter/filter.c:59-83), and the
-pipeline (filter/main.c:64-142) when the device is short of memory, which
-releases the filter's workspaces before ortho.
+"""The large-grid workload's path (the 4 nm sphere on a 192^3 grid) on a small
+case: the Newton filter at length 192 in both precisions (FP64 line passes;
+complex64 in the sub-plane form of the fused step) against the oracle
+(filter/filter.c:59-83), and the pipeline (filter/main.c:64-142) when the
+device is short of memory, which releases the filter's workspaces before
+ortho.
 
 Tolerances: FP64 filter 1e-9 relative; complex64 filter 1e-4 relative over
 16 Newton steps (FP32 rounding in the recursion, as the 36^3 mixed test);
