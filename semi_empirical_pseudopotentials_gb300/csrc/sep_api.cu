@@ -91,6 +91,7 @@ namespace sep {
 // the grid's tables and V in double-float, uploaded on first use
 int ensure_dd_grid(sep_ctx* c) {
   if (c->dd_ready) return kOk;
+  free_grid(c->gdd);  // what a failed earlier upload left
   RET(upload_grid<ddf>(c, c->gdd));
   if (c->have_pot) CK(convert_f64_to_dd(c->g64.pot, c->gdd.pot, c->n, c->stream));
   c->dd_ready = true;

@@ -1325,7 +1325,10 @@ int time_fused_step_device(sep_ctx* c, long npairs, int reps, double* ms_out) {
   int rc = kOk;
   for (int k = 0; k < 2 && rc == kOk; ++k) {
     for (int r = -1; r < reps && rc == kOk; ++r) {  // r = -1: warm-up
-      if (r == 0 && cudaEventRecord(e0, c->stream) != cudaSuccess) rc = arg_fail("event");
+      if (r == 0) {
+        const cudaError_t er = cudaEventRecord(e0, c->stream);
+        if (er != cudaSuccess) rc = cuda_fail(er, "cudaEventRecord", __LINE__);
+      }
       const cudaError_t e = k == 0 ? run_xy_pass(kInvEpiFwd, c->g32, io, (int)npairs, c->stream)
                                    : run_xy_zpass(c->g32, io, (int)npairs, c->stream);
       if (e != cudaSuccess) rc = cuda_fail(e, "fused step pass", __LINE__);

@@ -45,6 +45,19 @@ inline int pass_kind(int axis, int mode) {
 // lengths with a compiled line pass
 bool length_supported(int L);
 
+// SMs of the current device (152 if the query fails), read once per process
+inline int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0, v = 0;
+    n = (cudaGetDevice(&dev) == cudaSuccess &&
+         cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            ? v
+            : 152;
+  }
+  return n;
+}
+
 // buffers and scalars of one pass
 template <typename T> struct PassIO {
   cx<T>* data = nullptr;

@@ -7,17 +7,6 @@ namespace sep {
 
 namespace {
 
-int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
-      n = 152;
-  }
-  return n;
-}
-
 template <int L, int MODE>
 cudaError_t launch_sp(const PassArgs<float>& a, int B, cudaStream_t s) {
   using T = SpTune<L>;
