@@ -675,8 +675,11 @@ def run_sep(args):
     ctx.filter(start_np, an_re, zn, 4.0 / dE, vmin, out=out_np)  # warm the host path
     barrier()
     t0 = time.perf_counter()
+    calls = []
     for _ in range(args.steps):
+        tc = time.perf_counter()
         ctx.filter(start_np, an_re, zn, 4.0 / dE, vmin, out=out_np)
+        calls.append(time.perf_counter() - tc)
     barrier()
     t_e2e = time.perf_counter() - t0
     if dist:
@@ -684,7 +687,9 @@ def run_sep(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
     e2e = {"value": world * applies_step * args.steps / t_e2e, "unit": "applies/s",
-           "h2d_bytes_per_step": int(start_h.nbytes), "d2h_bytes_per_step": int(ns * ms * n * 8)}
+           "h2d_bytes_per_step": int(start_h.nbytes), "d2h_bytes_per_step": int(ns * ms * n * 8),
+           "host_call_s": [round(c, 4) for c in calls],
+           "device_resident_s_per_step": t_dev / args.steps}
 
     extras = {}
     if not args.no_extras and rank == 0:
