@@ -268,6 +268,8 @@ class Context:
         _check(lib().sep_ctx_set_graphs(self.h, 1 if enable else 0))
 
     def set_block_steps(self, k):
+        """Newton steps per accumulation pass, 1 <= k <= 128 (default 32); the
+        history holds k grids per pair of states."""
         _check(lib().sep_ctx_set_block_steps(self.h, int(k)))
 
     # -- stages
