@@ -608,6 +608,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def reduce_max(value, dist, device):
+    """The largest of the ranks' values: a replica run ends with its slowest
+    rank, so the whole job's time is the maximum over ranks (the value itself
+    with one rank)."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, applies_per_step, steps, seconds):
+    """Applies per second of the whole job: every replica filters the same
+    workload, so the job's work is world x the per-rank work."""
+    return world * applies_per_step * steps / seconds
+
+
 def run_sep(args):
     import torch
 
@@ -660,13 +679,9 @@ def run_sep(args):
         e1.record(stream)
         e1.synchronize()
     barrier()
-    t_dev = e0.elapsed_time(e1) * 1e-3
-    if dist:
-        tt = torch.tensor([t_dev], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
+    t_dev = reduce_max(e0.elapsed_time(e1) * 1e-3, dist, f"cuda:{local}")
     applies_step = ns * (nc - 1)
-    value = world * applies_step * args.steps / t_dev
+    value = whole_job_rate(world, applies_step, args.steps, t_dev)
 
     # e2e through the host-pointer call, pinned host buffers
     start_p = torch.from_numpy(start_h).pin_memory()
@@ -681,12 +696,8 @@ def run_sep(args):
         ctx.filter(start_np, an_re, zn, 4.0 / dE, vmin, out=out_np)
         calls.append(time.perf_counter() - tc)
     barrier()
-    t_e2e = time.perf_counter() - t0
-    if dist:
-        tt = torch.tensor([t_e2e], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e = {"value": world * applies_step * args.steps / t_e2e, "unit": "applies/s",
+    t_e2e = reduce_max(time.perf_counter() - t0, dist, f"cuda:{local}")
+    e2e = {"value": whole_job_rate(world, applies_step, args.steps, t_e2e), "unit": "applies/s",
            "h2d_bytes_per_step": int(start_h.nbytes), "d2h_bytes_per_step": int(ns * ms * n * 8),
            "host_call_s": [round(c, 4) for c in calls],
            "device_resident_s_per_step": t_dev / args.steps}
