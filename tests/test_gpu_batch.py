@@ -24,9 +24,10 @@ def _job(dims, seed, precision):
 
 @pytest.mark.parametrize("precision", ["f64", "mixed"])
 def test_batch_equals_single_runs(precision):
-    # (64, 64, 32): complex64 jobs of this shape run the fused xy plane pass
-    shapes = [(32, 32, 32), (36, 40, 48), (48, 48, 48), (64, 64, 32)]
-    ns, ms, nc = [3, 4, 2, 3], 3, 40
+    # complex64 jobs of (64, 64, 32) run the plane form of the fused step, of
+    # (96, 96, 96) the sub-plane form
+    shapes = [(32, 32, 32), (36, 40, 48), (48, 48, 48), (64, 64, 32), (96, 96, 96)]
+    ns, ms, nc = [3, 4, 2, 3, 2], 3, 40
     jobs = [_job(d, i, precision) for i, d in enumerate(shapes)]
     dE = 40.0
     singles, coefs = [], []
