@@ -23,7 +23,7 @@
 // of one residue x1 + (LZ / 8) x2): it does the y DFT_Rs and the z stage-A
 // DFT_8s of the block in registers, so a brick crosses shared memory twice,
 // as a z line pass does.  The sub-plane pass keeps x in the line passes'
-// split (N1 x 16) and its 20-, 24- or 32-row sub-planes (26 to 66 KB) in
+// split (N1 x N2) and its sub-planes of 14 to 32 rows (13 to 66 KB) in
 // shared memory, several blocks per SM.  Between passes x and y are kept in
 // digit-reversed position order (element k2 + N2 k1 of an axis at position
 // k1 + N1 k2), z in natural order; the k^2 tables follow the same order.
@@ -88,14 +88,14 @@ template <int L, int NT> struct SpShape {
 };
 
 // zy pass shape per length: TX adjacent columns per brick, threads per block,
-// blocks per SM.  A thread holds a 64-element block (about 160 registers); the
-// brick is LZ x 8 TX elements (33 to 131 KB).  Fastest measured (zy pass on
-// 0.5 GB of grids, fraction of the copy bandwidth): 96^3 (R = 4) TX 8 0.75,
-// 112^3 TX 8 0.64, 128^3 (R = 4) TX 8 0.74, 160^3 TX 4 0.48, 192^3 TX 4
-// 0.51, 256^3 TX 8 0.40.  With R = 8 the pass is
-// issue-bound (about 60 FP32 instructions per element for the two 8-point y
-// stages and the z transform pair) with 12 warps per SM; R = 4 needs about
-// 90 registers and no multiplies in its y stages.
+// blocks per SM.  A thread holds an R x 8 block (about 90 registers for
+// R = 4, 160 for R = 8); the brick is LZ x R TX elements (33 to 131 KB).
+// Fastest measured (zy pass on 0.5 GB of grids, fraction of the copy
+// bandwidth): 96^3 (R = 4) TX 8 0.75, 112^3 TX 8 0.64, 128^3 (R = 4) TX 8
+// 0.74, 160^3 TX 4 0.48, 192^3 TX 4 0.51, 256^3 TX 8 0.40.  With R = 8 the
+// pass is issue-bound (about 60 FP32 instructions per element for the two
+// 8-point y stages and the z transform pair) with 12 warps per SM; R = 4
+// needs no multiplies in its y stages and fits 20 warps per SM.
 template <int L> struct ZyTune {
   static constexpr int tx = 8, nt = 128, min_blocks = 1;
 };
