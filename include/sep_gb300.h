@@ -330,10 +330,10 @@ int sep_eigh_dev(double *a_dev, long n, double *w_dev, double *work_dev, void *c
  * of each Newton-step kernel on npairs complex grids in the context's
  * precision, over reps launches each: ms_out[0..6] = x forward, y forward,
  * z forward*k^2*inverse, y inverse, x inverse+epilogue+forward, accumulate
- * (block_steps history grids into ms = 8 state pairs), and the fused xy
- * plane pass (y/x inverse + epilogue + x/y forward; 0 when the context does
- * not use it).  No counterpart in the reference; used for the roofline
- * report. */
+ * (block_steps history grids into ms = 8 state pairs), and the fused step's
+ * xy pass (y/x inverse + epilogue + x/y forward, on planes or sub-planes; 0
+ * when the context has no fused step; sep_time_fused_step also times its z
+ * pass).  No counterpart in the reference; used for the roofline report. */
 int sep_time_passes(sep_ctx *ctx, long npairs, int reps, double *ms_out);
 /* The two passes of the fused complex64 Newton step (sep_ctx_set_fusion) on
  * npairs grids, average device ms per launch over reps launches: ms_out[0]

@@ -387,7 +387,8 @@ class Context:
 
     def time_passes(self, npairs, reps=10):
         """Average ms per launch: x fwd, y fwd, z fwd*k*inv, y inv, x inv+epi+fwd,
-        accumulate, and the fused xy plane pass (0 when it does not apply)."""
+        accumulate, and the fused step's xy pass (plane or sub-plane form; 0
+        when the context has no fused step)."""
         out = np.zeros(7)
         _check(lib().sep_time_passes(self.h, npairs, reps, _p(out)))
         return out
