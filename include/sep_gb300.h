@@ -193,6 +193,19 @@ int sep_pipeline(sep_ctx *ctx, const double *start, long ns, const double *el, l
                  long nc, double vmin, double dE, double *psi_out, double *eval,
                  double *sige, long *mkept, sep_timing *timing);
 
+/* ---- the filter's chunk plan (no counterpart in the reference) -----------
+ * How sep_filter splits `pairs` pairs of states (ceil(ns / 2)) into chunks of
+ * at most max_pairs (the pairs whose workspaces fit the device).  With host
+ * buffers (host_buffers != 0) each chunk's output copy runs under the next
+ * chunk's filter, so the last chunk splits off a tail: with a measured
+ * copy_ratio >= 0 (output copy time over filter time; a context measures it
+ * on each host-buffer call and uses it on the next) the smallest tail t >= 4
+ * with copy_ratio (c - t) <= t, at most half of it; with copy_ratio < 0 (not
+ * measured) the last chunk halves while it has 8 pairs or more.  counts: the
+ * chunks' pair counts in order (cap entries); *nchunks: their number. */
+int sep_filter_chunk_plan(long pairs, long max_pairs, int host_buffers, double copy_ratio,
+                          long *counts, long cap, long *nchunks);
+
 /* ---- host helpers, bit-identical to the reference -----------------------
  * filter/coeff.c:16-134: Newton coefficients of the Gaussian filters.
  * an_re, an_im: ms x nc; zn: nc. */

@@ -12,6 +12,7 @@ from .binding import (  # noqa: F401
     SepError,
     coefficients,
     device_count,
+    filter_chunk_plan,
     form_factor_backward,
     form_factor_table,
     hermitian_lowest,
@@ -20,6 +21,7 @@ from .binding import (  # noqa: F401
     start_states,
 )
 
-__all__ = ["Batch", "Context", "SepError", "coefficients", "device_count", "form_factor_backward", "form_factor_table",
+__all__ = ["Batch", "Context", "SepError", "coefficients", "device_count", "filter_chunk_plan",
+           "form_factor_backward", "form_factor_table",
            "hermitian_lowest", "ksqr",
            "lib", "start_states"]

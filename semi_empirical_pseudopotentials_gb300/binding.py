@@ -71,6 +71,8 @@ def lib():
         L.sep_sigma.argtypes = [vp, dp, C.c_long, dp]
         L.sep_pipeline.argtypes = [vp, dp, C.c_long, dp, C.c_long, C.c_long, C.c_double,
                                    C.c_double, dp, dp, dp, lp, C.POINTER(Timing)]
+        L.sep_filter_chunk_plan.argtypes = [C.c_long, C.c_long, C.c_int, C.c_double, lp,
+                                             C.c_long, lp]
         L.sep_coefficients.argtypes = [C.c_long, C.c_long, C.c_double, C.c_double, C.c_double,
                                        dp, dp, dp, dp]
         L.sep_start_states.argtypes = [C.c_long, C.c_long, C.c_long, C.c_double, dp]
@@ -154,6 +156,16 @@ def device_count():
     n = C.c_int()
     _check(lib().sep_device_count(C.byref(n)))
     return n.value
+
+
+def filter_chunk_plan(pairs, max_pairs, host_buffers=True, copy_ratio=-1.0):
+    """Pair counts of the chunks sep_filter runs (see sep_filter_chunk_plan)."""
+    counts = np.zeros(64, dtype=np.int64)
+    nchunks = C.c_long(0)
+    _check(lib().sep_filter_chunk_plan(int(pairs), int(max_pairs), 1 if host_buffers else 0,
+                                       float(copy_ratio), counts.ctypes.data_as(lp), 64,
+                                       C.byref(nchunks)))
+    return [int(x) for x in counts[:nchunks.value]]
 
 
 # ---- host helpers (bit-identical to the reference) --------------------------

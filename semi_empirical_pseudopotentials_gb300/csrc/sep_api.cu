@@ -814,6 +814,17 @@ int sep_subspace_rotate(sep_ctx* c, const double* W, const double* X, long m, lo
 }
 
 // ---- host helpers --------------------------------------------------------
+int sep_filter_chunk_plan(long pairs, long max_pairs, int host_buffers, double copy_ratio,
+                          long* counts, long cap, long* nchunks) {
+  if (pairs < 1 || max_pairs < 1 || !counts || !nchunks || cap < 1 || std::isnan(copy_ratio))
+    return arg_fail("sep_filter_chunk_plan: bad argument");
+  const auto plan = host::filter_chunks(pairs, max_pairs, host_buffers != 0, copy_ratio);
+  *nchunks = (long)plan.size();
+  if ((long)plan.size() > cap) return arg_fail("sep_filter_chunk_plan: cap too small");
+  for (size_t k = 0; k < plan.size(); ++k) counts[k] = (long)plan[k].second;
+  return kOk;
+}
+
 int sep_coefficients(long ms, long nc, double dE, double vmin, double dt, const double* el,
                      double* an_re, double* an_im, double* zn) {
   if (ms < 1 || nc < 1 || !el || !an_re || !an_im || !zn || !(dE > 0.0))

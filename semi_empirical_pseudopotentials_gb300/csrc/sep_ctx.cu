@@ -272,26 +272,8 @@ int filter_impl(sep_ctx* c, const double* d_start, long ns, const double* an_re,
   //    r (c - t) <= t (32 pairs at r = 0.06: 28 + 4);
   //  - not measured yet: halved while it has 8 pairs or more (32 pairs:
   //    16, 8, 4, 4), which overlaps the copies even when they are slow.
-  std::vector<std::pair<long long, long long>> chunks;
-  for (long long b0 = 0; b0 < B; b0 += Bc) chunks.push_back({b0, std::min<long long>(Bc, B - b0)});
-  if (host && c->host_copy_ratio >= 0.0) {
-    auto& last = chunks.back();
-    if (last.second >= 8) {
-      const double r = c->host_copy_ratio;
-      long long t = (long long)std::ceil(r * (double)last.second / (1.0 + r));
-      t = std::max<long long>(t, 4);
-      t = std::min<long long>(t, last.second / 2);
-      last.second -= t;
-      chunks.push_back({last.first + last.second, t});
-    }
-  } else if (host) {
-    while (chunks.back().second >= 8) {
-      auto& last = chunks.back();
-      const long long second = last.second / 2;
-      last.second -= second;
-      chunks.push_back({last.first + last.second, second});
-    }
-  }
+  const std::vector<std::pair<long long, long long>> chunks =
+      host::filter_chunks(B, Bc, host != nullptr, c->host_copy_ratio);
   const long long nchunks = (long long)chunks.size();
   std::vector<cudaEvent_t> ev;  // per chunk: start states up, output computed
   // timing of chunk 0: filter (on the stream) and output copy (on d2h)

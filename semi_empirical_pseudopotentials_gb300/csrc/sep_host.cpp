@@ -319,5 +319,32 @@ std::vector<double> axis_coords(long n, double min, double step) {
   return c;
 }
 
+std::vector<std::pair<long long, long long>> filter_chunks(long long pairs, long long bc,
+                                                           bool host, double ratio) {
+  std::vector<std::pair<long long, long long>> chunks;
+  if (pairs < 1 || bc < 1) return chunks;
+  for (long long b0 = 0; b0 < pairs; b0 += bc)
+    chunks.push_back({b0, std::min<long long>(bc, pairs - b0)});
+  if (!host) return chunks;
+  if (ratio >= 0.0) {
+    auto& last = chunks.back();
+    if (last.second >= 8) {
+      long long t = (long long)std::ceil(ratio * (double)last.second / (1.0 + ratio));
+      t = std::max<long long>(t, 4);
+      t = std::min<long long>(t, last.second / 2);
+      last.second -= t;
+      chunks.push_back({last.first + last.second, t});
+    }
+  } else {
+    while (chunks.back().second >= 8) {
+      auto& last = chunks.back();
+      const long long second = last.second / 2;
+      last.second -= second;
+      chunks.push_back({last.first + last.second, second});
+    }
+  }
+  return chunks;
+}
+
 }  // namespace host
 }  // namespace sep

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 namespace sep {
@@ -46,6 +47,17 @@ void form_factor_table(const double a[4], double vol_per_atom, double* r, double
 
 // filter/init.c:157-159 grid coordinates (running sums from the minimum)
 std::vector<double> axis_coords(long n, double min, double step);
+
+// The filter's chunks of pairs (first, count): at most bc each.  With host
+// buffers each chunk's output copy runs under the next chunk's filter and the
+// last chunk's copy is not overlapped; small chunks filter fewer pairs per
+// second, so the last chunk splits off a tail:
+//  - ratio >= 0 (output copy time over filter time per pair, measured by an
+//    earlier call): the smallest tail t >= 4 with ratio (c - t) <= t, at most
+//    half the chunk;
+//  - ratio < 0 (not measured yet): halved while it has 8 pairs or more.
+std::vector<std::pair<long long, long long>> filter_chunks(long long pairs, long long bc,
+                                                           bool host, double ratio);
 
 }  // namespace host
 }  // namespace sep
